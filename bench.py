@@ -1,0 +1,396 @@
+#!/usr/bin/env python3
+"""Benchmark: malloc+free pairs per second of the device allocator on GB300.
+
+Default workload (the reference metric's mixed-size configuration): an 8 GiB
+arena of 16 MiB segments, Gallatin<16 MiB, 16, 4096>; 4,194,304 threads, each
+for 8 rounds mallocs 16 << k bytes (k = x mod 9 of a per-thread xorshift64
+seeded by splitmix64(42 + tid)), fills every 16 bytes with tid ^ round,
+verifies and frees; plus 256 segment-tier requests of 16-256 MiB (thread 0
+of every 64th 256-thread CTA). One step = one launch of that workload kernel.
+`--workload pairs` runs the small plain configuration instead: a 2 GiB arena,
+1,048,576 threads (1024 x 1024), malloc 16 B / store tid / verify / free.
+
+value: pairs/s with the class trace resident in HBM, device time from CUDA
+events on the launching stream, L2 flushed (256 MiB write) before every
+timed step. e2e: the same metric through the C-ABI host-buffer entry point
+(gal_run_mixed_host): the pinned host class trace is copied to the device,
+the kernel runs, the stats words come back, all inside the timed region.
+
+--impl reference runs the reference's own CUDA build (oracle/_ref, the
+reference headers compiled for sm_103a) through the same workload kernels.
+Under torchrun every rank runs an independent replica (the allocator is one
+arena per GPU: replicas only, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+GIB = 1 << 30
+MIB = 1 << 20
+WORKLOADS = {
+    "mixed": dict(
+        arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=4_194_304, rounds=8, block=256,
+        seg_every=64, seg_lo=16 * MIB, seg_hi=256 * MIB,
+    ),
+    "pairs": dict(arena=2 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=1_048_576, size=16, block=1024),
+}
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    QUERY = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+            )
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        else:
+            self.lines = []
+
+    def summary(self) -> dict:
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                maxes.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {
+            "sm_mhz": statistics.median(sms) if sms else None,
+            "sm_max_mhz": max(maxes) if maxes else None,
+            "reasons": sorted(reasons),
+            "samples": len(sms),
+        }
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier_max(torch, world: int, value: float) -> float:
+    if world == 1:
+        return value
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(torch, world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def make_allocator(impl: str, w: dict):
+    if impl == "reference":
+        import oracle
+
+        return oracle.RefGallatin(w["arena"], 42, w["segment"], w["min_size"], w["max_size"])
+    import gallatin_gb300 as gal
+
+    return gal.Gallatin.generate_on_device(
+        w["arena"], 42, print_info=False, segment_size=w["segment"], min_size=w["min_size"], max_size=w["max_size"]
+    )
+
+
+def close_allocator(impl: str, a) -> None:
+    if impl == "reference":
+        a.close()
+    else:
+        a.free_on_device()
+
+
+def cpu_baseline(name: str, w: dict) -> dict:
+    """glibc malloc/free replay of the same trace on this host's cores."""
+    import oracle
+
+    cores = os.cpu_count() or 1
+    if name == "mixed":
+        n, rounds = w["threads"], w["rounds"]
+        secs, misses, bad = oracle.cpu_replay_mixed(
+            n, 0, n, rounds, 42, seg_every=w["seg_every"], block_dim=w["block"], seg_lo=w["seg_lo"],
+            seg_hi=w["seg_hi"], workers=cores,
+        )
+        units = n * rounds + n // w["block"] // w["seg_every"]
+        sample = f"full workload: {n} threads x {rounds} rounds + segment-tier requests, glibc malloc/free"
+    else:
+        n = w["threads"]
+        secs, misses, bad = oracle.cpu_replay_pairs(n, w["size"], cores)
+        units = n
+        sample = f"full workload: {n} threads, glibc malloc/free of {w['size']} B"
+    return {
+        "value": units / secs,
+        "unit": "malloc+free pairs/s",
+        "cores": cores,
+        "kind": "port",
+        "sample": sample + " (the reference has no CPU implementation; this replays the trace through glibc)",
+        "seconds": secs,
+        "misses": misses,
+        "verify_failures": bad,
+    }
+
+
+def run(args) -> dict | None:
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    w = WORKLOADS[args.workload]
+    impl = args.impl
+    if impl == "reference":
+        import oracle
+
+        if oracle.load_ref() is None:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "reference CUDA build (oracle/_ref) is not built"}))
+            return None
+    else:
+        import gallatin_gb300 as gal
+
+        gal.load()
+
+    stream = torch.cuda.current_stream()
+    s_ptr = stream.cuda_stream
+    a = make_allocator(impl, w)
+    stats = torch.zeros(8, dtype=torch.int64, device="cuda")
+    flush = torch.empty(256 * MIB, dtype=torch.uint8, device="cuda")
+
+    if args.workload == "mixed":
+        from gallatin_gb300.workload import mixed_class_trace, mixed_mean_bytes
+
+        n, rounds = w["threads"], w["rounds"]
+        trace = mixed_class_trace(n, rounds, 42)
+        d_trace = torch.from_numpy(trace.reshape(-1)).cuda()
+        h_trace = torch.from_numpy(trace.reshape(-1)).pin_memory()
+        seg_requests = n // w["block"] // w["seg_every"]
+        units = n * rounds + seg_requests
+        alg_bytes = n * rounds * 2 * mixed_mean_bytes() + seg_requests * 64
+
+        def step():
+            a.run_mixed(n, rounds, 42, stats.data_ptr(), seg_every=w["seg_every"], seg_lo=w["seg_lo"],
+                        seg_hi=w["seg_hi"], d_classes=d_trace.data_ptr(), block_dim=w["block"], stream=s_ptr)
+
+        def e2e_step():
+            return a.run_mixed_host(n, rounds, 42, h_trace.data_ptr(), seg_every=w["seg_every"],
+                                    seg_lo=w["seg_lo"], seg_hi=w["seg_hi"], block_dim=w["block"], stream=s_ptr)
+
+        h2d = n * rounds
+        config = {
+            "workload": "mixed sizes 16..4096 B powers of two, 8 rounds malloc/fill/verify/free",
+            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+            "max_size": w["max_size"], "threads": n, "rounds": rounds, "block_dim": w["block"],
+            "segment_tier_requests": seg_requests, "segment_tier_bytes": [w["seg_lo"], w["seg_hi"]], "seed": 42,
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
+    else:
+        n = w["threads"]
+        units = n
+        alg_bytes = n * 16
+
+        def step():
+            a.run_pairs(n, w["size"], stats.data_ptr(), block_dim=w["block"], stream=s_ptr)
+
+        e2e_step = None
+        h2d = 0
+        config = {
+            "workload": "plain 16 B malloc/store/verify/free", "arena_bytes": w["arena"], "segment_bytes": w["segment"],
+            "min_size": w["min_size"], "max_size": w["max_size"], "threads": n, "block_dim": w["block"], "seed": 42,
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stats.zero_()
+
+    times = []
+    barrier(torch, world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            step()
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1))
+        torch.cuda.synchronize()
+    barrier(torch, world)
+    st = stats.cpu().numpy()
+    total_ms = barrier_max(torch, world, float(sum(times)))
+    ms_per_step = total_ms / args.steps
+    value = units * args.steps * world / (total_ms / 1e3)
+
+    e2e = None
+    if e2e_step is not None and not args.no_e2e:
+        e2e_step()  # grow scratch buffers outside the timed region
+        torch.cuda.synchronize()
+        e2e_times = []
+        e2e_bad = np.zeros(8, dtype=np.uint64)
+        barrier(torch, world)
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = e2e_step()
+            e2e_times.append(time.perf_counter() - t0)
+            e2e_bad += out
+        e2e_total = barrier_max(torch, world, float(sum(e2e_times)))
+        e2e = {
+            "value": units * args.steps * world / e2e_total,
+            "unit": "malloc+free pairs/s",
+            "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": 64,
+            "ms_per_step": 1e3 * e2e_total / args.steps,
+            "misses": int(e2e_bad[0]),
+            "verify_failures": int(e2e_bad[1]),
+        }
+
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    achieved = alg_bytes / (ms_per_step / 1e3) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": peak if peak else 6800.0,
+        "unit": "GB/s",
+        "frac": achieved / (peak if peak else 6800.0),
+        "traffic": None,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peak else "fallback 6.8 TB/s",
+        "algorithmic_bytes_per_launch": alg_bytes,
+    }
+    traffic_file = REPO / "profiles" / f"traffic_{impl}_{args.workload}.json"
+    if traffic_file.exists():
+        try:
+            roofline["traffic"] = json.loads(traffic_file.read_text()).get("dram_bytes_per_launch")
+        except ValueError:
+            pass
+
+    result = {
+        "metric": "malloc+free ops/s (one op = one malloc + its free)",
+        "value": value,
+        "unit": "malloc+free pairs/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64",
+        "data": "synthetic (seeded xorshift64 size trace; no dataset)",
+        "config": config,
+        "impl": impl,
+        "roofline": roofline,
+        "e2e": e2e,
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+        "misses": int(st[0]),
+        "verify_failures": int(st[1]),
+        "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
+        "step_ms": times,
+    }
+    if impl == "gb300":
+        result["allocator_counters"] = a.stats()["counters"]
+    close_allocator(impl, a)
+    if rank == 0 and impl == "gb300" and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(args.workload, w)
+    if impl == "reference":
+        result["cpu_baseline"] = {
+            "value": value, "unit": "malloc+free pairs/s", "cores": 0, "kind": "reference",
+            "sample": "the reference's own CUDA build on this GPU (it has no CPU path), full workload",
+        }
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return result if rank == 0 else None
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mixed")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    res = run(args)
+    if res is not None:
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -1,0 +1,446 @@
+"""GB300-native Gallatin device allocator: host-side Python mirror of the C ABI.
+
+The allocator itself is CUDA code: device malloc/free are header-only
+(include/gallatin/allocators/gallatin.cuh) and the host library
+libgallatin_gb300.so (include/gallatin_gb300.h) builds, inspects and destroys
+allocator state and runs batch kernels over it. This module binds that
+library with ctypes and mirrors the reference's host interface
+(gallatin::allocators::Gallatin<seg, min, max>::generate_on_device /
+free_on_device / print_info, and init_global_allocator / free_global_allocator
+/ print_global_stats from global_allocator.cuh:48-97).
+
+Device buffers are passed as integer device addresses and streams as integer
+cudaStream_t handles, so any CUDA buffer provider works (the tests use torch).
+There is no CPU fallback: without the compiled library every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_int, c_int64, c_uint8, c_uint32, c_uint64, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from . import _build
+
+__all__ = [
+    "GalError",
+    "Gallatin",
+    "VebTree",
+    "load",
+    "lib_path",
+    "init_global_allocator",
+    "free_global_allocator",
+    "print_global_stats",
+    "global_allocator",
+    "OPS",
+    "DUMP",
+    "COUNTERS",
+    "classify",
+]
+
+GAL_MAX_TREES = 24
+GAL_NUM_COUNTERS = 16
+GAL_EMPTY_BLOCK = 0xFFFFFFFF
+GAL_FREE_SEGMENT = 0xFFFF
+GAL_SEG_GATE = -(1 << 28)
+
+OPS = {
+    "insert": 0,
+    "insert_force_update": 1,
+    "remove": 2,
+    "query": 3,
+    "successor": 4,
+    "successor_thorough": 5,
+    "lock_offset": 6,
+    "malloc_first": 7,
+    "find_first_valid_index": 8,
+    "find_random_valid_index": 9,
+    "malloc": 10,
+    "gather_multiple": 11,
+    "return_multiple": 12,
+    "report_fill": 13,
+}
+
+DUMP = {
+    "chunk_ids": (0, np.uint16),
+    "seg_avail": (1, np.int32),
+    "seg_block_bits": (2, np.uint64),
+    "block_meta": (3, np.uint64),
+    "block_bits": (4, np.uint64),
+    "block_ext": (5, np.uint64),
+    "slots": (6, np.uint64),
+    "counters": (7, np.uint64),
+    "segment_tree": (8, np.uint64),
+    "sub_tree": (9, np.uint64),
+    "locks": (10, np.uint32),
+}
+
+COUNTERS = [
+    "oom_slice",
+    "oom_block",
+    "oom_segment",
+    "timeout",
+    "bad_free",
+    "corrupt",
+    "block_pins",
+    "segment_attach",
+    "segment_retire",
+    "block_retire",
+]
+
+
+class GalError(RuntimeError):
+    """A C-ABI call returned an error status."""
+
+
+class _Geometry(ctypes.Structure):
+    _fields_ = [
+        ("segment_bytes", c_uint64),
+        ("min_size", c_uint64),
+        ("max_size", c_uint64),
+        ("num_segments", c_uint64),
+        ("arena_bytes", c_uint64),
+        ("num_trees", c_uint32),
+        ("blocks_per_segment", c_uint32),
+        ("num_sms", c_uint32),
+        ("total_slots", c_uint32),
+        ("slot_count", c_uint32 * GAL_MAX_TREES),
+        ("arena_base", c_uint64),
+    ]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [
+        ("num_segments", c_uint64),
+        ("free_segments", c_uint64),
+        ("tree_segments", c_uint64 * GAL_MAX_TREES),
+        ("tree_blocks_out", c_uint64 * GAL_MAX_TREES),
+        ("tree_live_slices", c_uint64 * GAL_MAX_TREES),
+        ("segment_allocations", c_uint64),
+        ("segments_in_allocations", c_uint64),
+        ("counters", c_uint64 * GAL_NUM_COUNTERS),
+    ]
+
+
+VEB_OP_DTYPE = np.dtype([("code", "<u4"), ("tid", "<u4"), ("arg", "<u8"), ("arg2", "<u8")])
+
+_LIB = None
+
+
+def lib_path() -> Path:
+    return _build.lib_path()
+
+
+def load(path: str | Path | None = None):
+    """Load the compiled C-ABI library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = Path(path) if path else lib_path()
+    if not p.exists():
+        raise GalError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(p))
+    vp, u64, u32, i32 = c_void_p, c_uint64, c_uint32, c_int
+    sigs = {
+        "gal_create": (i32, [u64, u64, u64, u64, u64, u32, POINTER(vp)]),
+        "gal_destroy": (i32, [vp]),
+        "gal_device_state": (vp, [vp]),
+        "gal_from_device_state": (vp, [vp]),
+        "gal_geometry": (i32, [vp, POINTER(_Geometry)]),
+        "gal_stats": (i32, [vp, POINTER(_Stats)]),
+        "gal_print_info": (i32, [vp]),
+        "gal_reset_counters": (i32, [vp]),
+        "gal_dump_bytes": (c_int64, [vp, i32, i32, i32]),
+        "gal_dump": (i32, [vp, i32, i32, i32, vp, u64]),
+        "gal_veb_layer_count": (i32, [vp, i32]),
+        "gal_malloc_batch": (i32, [vp, vp, u64, vp, vp]),
+        "gal_free_batch": (i32, [vp, vp, u64, vp]),
+        "gal_flush_pinned": (i32, [vp, vp]),
+        "gal_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
+        "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
+        "gal_veb_destroy": (i32, [vp]),
+        "gal_veb_num_layers": (i32, [vp]),
+        "gal_veb_layer_words": (u64, [vp, i32]),
+        "gal_veb_dump": (i32, [vp, i32, vp]),
+        "gal_veb_run_ops": (i32, [vp, vp, u64, vp, vp]),
+        "gal_last_error": (c_char_p, []),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        msg = load().gal_last_error().decode(errors="replace")
+        raise GalError(f"gallatin_gb300 call failed ({rc}): {msg}")
+
+
+def _ceil_log2(v: int) -> int:
+    return (v - 1).bit_length() if v > 1 else 0
+
+
+def classify(size: int, min_size: int = 16, max_size: int = 4096, segment_size: int = 16 << 20):
+    """Tier of a request, as the device dispatch computes it.
+
+    Returns (tier, tree, count_or_nseg) with tier in {"slice", "block",
+    "segment"} (reference gallatin.cuh:1141-1147, 1196-1260)."""
+    min_shift = min_size.bit_length() - 1
+    max_shift = max_size.bit_length() - 1
+    num_trees = max_shift - min_shift + 1
+    block_shift_min = min_shift + 12
+    if size < min_size:
+        return ("slice", 0, 1)
+    cl = _ceil_log2(size)
+    tree = cl - min_shift
+    if tree < num_trees:
+        return ("slice", tree, 1)
+    bt = cl - block_shift_min
+    if bt < 0:
+        return ("slice", num_trees - 1, 1 << (tree - (num_trees - 1)))
+    if bt < num_trees:
+        return ("block", bt, 1)
+    return ("segment", 0, (size - 1) // segment_size + 1)
+
+
+class Gallatin:
+    """Host handle of one device allocator (reference Gallatin<seg, min, max>)."""
+
+    def __init__(self, handle: int, segment_size: int, min_size: int, max_size: int):
+        self._h = handle
+        self.segment_size = segment_size
+        self.min_size = min_size
+        self.max_size = max_size
+        g = _Geometry()
+        _check(load().gal_geometry(self._h, ctypes.byref(g)))
+        self.num_segments = g.num_segments
+        self.arena_bytes = g.arena_bytes
+        self.num_trees = g.num_trees
+        self.blocks_per_segment = g.blocks_per_segment
+        self.num_sms = g.num_sms
+        self.total_slots = g.total_slots
+        self.slot_count = list(g.slot_count)[: g.num_trees]
+        self.arena_base = g.arena_base
+
+    @classmethod
+    def generate_on_device(
+        cls,
+        max_bytes: int,
+        seed: int,
+        print_info: bool = True,
+        running_calloc: bool = False,
+        *,
+        segment_size: int = 16 << 20,
+        min_size: int = 16,
+        max_size: int = 4096,
+        min_slots: int = 0,
+    ) -> "Gallatin":
+        del running_calloc  # calloc via dynamic parallelism is not provided
+        h = c_void_p()
+        _check(load().gal_create(max_bytes, seed, segment_size, min_size, max_size, min_slots, ctypes.byref(h)))
+        obj = cls(h.value, segment_size, min_size, max_size)
+        if print_info:
+            print(
+                f"Booted Gallatin with {obj.num_trees} trees in range {min_size}-{max_size} and "
+                f"{max_bytes / 2**30:f} GB of memory {obj.num_segments} segments"
+            )
+        return obj
+
+    def free_on_device(self) -> None:
+        if self._h:
+            _check(load().gal_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free_on_device()
+
+    @property
+    def handle(self) -> int:
+        if not self._h:
+            raise GalError("allocator already freed")
+        return self._h
+
+    @property
+    def device_ptr(self) -> int:
+        """Device pointer user kernels receive (what generate_on_device returns in C++)."""
+        return load().gal_device_state(self.handle)
+
+    # -- batch device entry points ------------------------------------------
+    def malloc_batch(self, d_sizes: int, n: int, d_ptrs: int, stream: int = 0) -> None:
+        _check(load().gal_malloc_batch(self.handle, d_sizes, n, d_ptrs, stream))
+
+    def free_batch(self, d_ptrs: int, n: int, stream: int = 0) -> None:
+        _check(load().gal_free_batch(self.handle, d_ptrs, n, stream))
+
+    def flush_pinned(self, stream: int = 0) -> None:
+        _check(load().gal_flush_pinned(self.handle, stream))
+
+    def run_pairs(self, n_threads: int, size: int, d_stats: int, block_dim: int = 1024, stream: int = 0) -> None:
+        _check(load().gal_run_pairs(self.handle, n_threads, size, block_dim, d_stats, stream))
+
+    def run_mixed(
+        self,
+        n_threads: int,
+        rounds: int,
+        seed: int,
+        d_stats: int,
+        *,
+        seg_every: int = 0,
+        seg_lo: int = 16 << 20,
+        seg_hi: int = 256 << 20,
+        d_classes: int = 0,
+        block_dim: int = 256,
+        stream: int = 0,
+    ) -> None:
+        _check(
+            load().gal_run_mixed(
+                self.handle, n_threads, rounds, seed, seg_every, seg_lo, seg_hi, d_classes, block_dim, d_stats, stream
+            )
+        )
+
+    def run_mixed_host(
+        self,
+        n_threads: int,
+        rounds: int,
+        seed: int,
+        h_classes_ptr: int,
+        *,
+        seg_every: int = 0,
+        seg_lo: int = 16 << 20,
+        seg_hi: int = 256 << 20,
+        block_dim: int = 256,
+        stream: int = 0,
+    ) -> np.ndarray:
+        out = np.zeros(8, dtype=np.uint64)
+        _check(
+            load().gal_run_mixed_host(
+                self.handle,
+                n_threads,
+                rounds,
+                seed,
+                seg_every,
+                seg_lo,
+                seg_hi,
+                h_classes_ptr,
+                block_dim,
+                out.ctypes.data,
+                stream,
+            )
+        )
+        return out
+
+    # -- inspection -----------------------------------------------------------
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(load().gal_stats(self.handle, ctypes.byref(s)))
+        nt = self.num_trees
+        return {
+            "num_segments": s.num_segments,
+            "free_segments": s.free_segments,
+            "tree_segments": list(s.tree_segments)[:nt],
+            "tree_blocks_out": list(s.tree_blocks_out)[:nt],
+            "tree_live_slices": list(s.tree_live_slices)[:nt],
+            "segment_allocations": s.segment_allocations,
+            "segments_in_allocations": s.segments_in_allocations,
+            "counters": dict(zip(COUNTERS, list(s.counters)[: len(COUNTERS)])),
+        }
+
+    def print_info(self) -> None:
+        _check(load().gal_print_info(self.handle))
+
+    def reset_counters(self) -> None:
+        _check(load().gal_reset_counters(self.handle))
+
+    def dump(self, name: str, tree: int = 0, layer: int = 0) -> np.ndarray:
+        which, dtype = DUMP[name]
+        nbytes = load().gal_dump_bytes(self.handle, which, tree, layer)
+        if nbytes < 0:
+            raise GalError(f"no dump target {name} tree={tree} layer={layer}")
+        out = np.empty(nbytes // np.dtype(dtype).itemsize, dtype=dtype)
+        _check(load().gal_dump(self.handle, which, tree, layer, out.ctypes.data, nbytes))
+        return out
+
+    def veb_layers(self, tree: int = -1) -> list[np.ndarray]:
+        """All layers (top first) of the segment tree (tree=-1) or sub tree `tree`."""
+        n = load().gal_veb_layer_count(self.handle, tree)
+        if tree < 0:
+            return [self.dump("segment_tree", 0, i) for i in range(n)]
+        return [self.dump("sub_tree", tree, i) for i in range(n)]
+
+
+class VebTree:
+    """Standalone device vEB tree (reference veb_tree, veb.cuh:528-1228)."""
+
+    def __init__(self, universe: int, seed: int):
+        h = c_void_p()
+        _check(load().gal_veb_create(universe, seed, ctypes.byref(h)))
+        self._h = h.value
+        self.universe = universe
+        self.seed = seed
+
+    def close(self) -> None:
+        if self._h:
+            _check(load().gal_veb_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def num_layers(self) -> int:
+        return load().gal_veb_num_layers(self._h)
+
+    def layers(self) -> list[np.ndarray]:
+        out = []
+        for layer in range(self.num_layers):
+            words = load().gal_veb_layer_words(self._h, layer)
+            arr = np.empty(words, dtype=np.uint64)
+            _check(load().gal_veb_dump(self._h, layer, arr.ctypes.data))
+            out.append(arr)
+        return out
+
+    def run_ops(self, d_ops: int, n: int, d_results: int, stream: int = 0) -> None:
+        _check(load().gal_veb_run_ops(self._h, d_ops, n, d_results, stream))
+
+
+# -- global allocator (reference global_allocator.cuh:41-97) -----------------
+_GLOBAL: Gallatin | None = None
+
+
+def init_global_allocator(num_bytes: int, seed: int, print_info: bool = True, running_calloc: bool = False) -> Gallatin:
+    """Create the process-wide Gallatin<16 MiB, 16, 4096> allocator."""
+    global _GLOBAL
+    if _GLOBAL is not None:
+        _GLOBAL.free_on_device()
+    _GLOBAL = Gallatin.generate_on_device(num_bytes, seed, print_info, running_calloc)
+    return _GLOBAL
+
+
+def global_allocator() -> Gallatin:
+    if _GLOBAL is None:
+        raise GalError("init_global_allocator has not been called")
+    return _GLOBAL
+
+
+def free_global_allocator() -> None:
+    global _GLOBAL
+    if _GLOBAL is not None:
+        _GLOBAL.free_on_device()
+        _GLOBAL = None
+
+
+def print_global_stats() -> None:
+    global_allocator().print_info()

@@ -1,0 +1,51 @@
+// Host-side definitions shared by the C-ABI translation units.
+#ifndef GALLATIN_GB300_CAPI_INTERNAL_H
+#define GALLATIN_GB300_CAPI_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "gallatin_gb300.h"
+
+struct gal_allocator {
+  gal_state_t hs;         // host copy; pointers are device addresses
+  gal_state_t *d_state;   // device copy user kernels receive
+  uint64_t min_size;
+  uint64_t max_size;
+  std::vector<void *> device_allocs;
+  // scratch for the host-buffer entry points, grown on demand
+  uint8_t *d_classes;
+  uint64_t d_classes_bytes;
+  unsigned long long *d_stats;
+};
+
+struct gal_veb {
+  gal_veb_t hv;
+  gal_veb_t *d_veb;
+  std::vector<void *> device_allocs;
+};
+
+namespace galcapi {
+
+// Record a failed CUDA call; returns GAL_ERR_CUDA (or GAL_ERR_NOMEM for
+// allocation failures) so callers can `return fail(...)`.
+int fail_cuda(cudaError_t e, const char *what);
+int fail_invalid(const char *what);
+void set_error(const char *msg);
+
+// Build vEB layers on the device; `full` sets every id < universe.
+int build_veb(gal_veb_t *t, uint64_t universe, uint64_t seed, bool full, std::vector<void *> &allocs);
+
+inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace galcapi
+
+#define GAL_CUDA_TRY(call, what)                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return galcapi::fail_cuda(e_, what); \
+  } while (0)
+
+#endif  // GALLATIN_GB300_CAPI_INTERNAL_H

@@ -1,0 +1,115 @@
+// C ABI: batch malloc/free, pinned-block flush, and the benchmark workloads,
+// all launched over the device allocator inlined from alloc.cuh.
+#include <cuda_runtime.h>
+
+#include "capi_internal.h"
+#include "gallatin_gb300/alloc.cuh"
+#include "workloads.cuh"
+
+namespace {
+
+// The device allocator seen through the malloc/free interface the workload
+// templates expect; same layout as gal_state_t.
+struct gal_device_alloc {
+  gal_state_t state;
+  __device__ __forceinline__ void *malloc(uint64_t n) { return gal::malloc(&state, n); }
+  __device__ __forceinline__ void free(void *p) { gal::free(&state, p); }
+};
+
+__global__ void malloc_batch_kernel(const gal_state_t *st, const uint64_t *sizes, uint64_t n, uint64_t *out) {
+  const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  out[tid] = (uint64_t)gal::malloc(st, sizes[tid]);
+}
+
+__global__ void free_batch_kernel(const gal_state_t *st, const uint64_t *ptrs, uint64_t n) {
+  const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  gal::free(st, (void *)ptrs[tid]);
+}
+
+__global__ void flush_kernel(const gal_state_t *st, uint32_t total_slots) {
+  const uint32_t tid = threadIdx.x + blockIdx.x * blockDim.x;
+  if (tid >= total_slots) return;
+  gal::flush_slot(st, st->slots + tid);
+}
+
+cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+}  // namespace
+
+using galcapi::fail_invalid;
+using galcapi::grid_for;
+
+extern "C" int gal_malloc_batch(gal_allocator *h, const uint64_t *d_sizes, uint64_t n, uint64_t *d_ptrs,
+                                void *stream) {
+  if (h == nullptr || (n && (d_sizes == nullptr || d_ptrs == nullptr))) return fail_invalid("NULL argument");
+  if (n == 0) return GAL_OK;
+  malloc_batch_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(h->d_state, d_sizes, n, d_ptrs);
+  GAL_CUDA_TRY(cudaGetLastError(), "malloc_batch launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_free_batch(gal_allocator *h, const uint64_t *d_ptrs, uint64_t n, void *stream) {
+  if (h == nullptr || (n && d_ptrs == nullptr)) return fail_invalid("NULL argument");
+  if (n == 0) return GAL_OK;
+  free_batch_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(h->d_state, d_ptrs, n);
+  GAL_CUDA_TRY(cudaGetLastError(), "free_batch launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_flush_pinned(gal_allocator *h, void *stream) {
+  if (h == nullptr) return fail_invalid("handle is NULL");
+  const uint32_t total = h->hs.total_slots;
+  flush_kernel<<<grid_for(total, 128), 128, 0, as_stream(stream)>>>(h->d_state, total);
+  GAL_CUDA_TRY(cudaGetLastError(), "flush launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_run_pairs(gal_allocator *h, uint64_t n_threads, uint64_t size, uint32_t block_dim,
+                             unsigned long long *d_stats, void *stream) {
+  if (h == nullptr || d_stats == nullptr) return fail_invalid("NULL argument");
+  if (block_dim == 0 || block_dim > 1024 || block_dim % 32) return fail_invalid("block_dim must be 32..1024, x32");
+  if (n_threads == 0) return GAL_OK;
+  galwork::pairs_kernel<gal_device_alloc><<<grid_for(n_threads, block_dim), block_dim, 0, as_stream(stream)>>>(
+      reinterpret_cast<gal_device_alloc *>(h->d_state), n_threads, size, d_stats);
+  GAL_CUDA_TRY(cudaGetLastError(), "pairs launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_run_mixed(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
+                             uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *d_classes,
+                             uint32_t block_dim, unsigned long long *d_stats, void *stream) {
+  if (h == nullptr || d_stats == nullptr) return fail_invalid("NULL argument");
+  if (block_dim == 0 || block_dim > 1024 || block_dim % 32) return fail_invalid("block_dim must be 32..1024, x32");
+  if (seg_every && (seg_lo == 0 || seg_hi < seg_lo)) return fail_invalid("bad segment-tier size range");
+  if (n_threads == 0) return GAL_OK;
+  galwork::mixed_kernel<gal_device_alloc><<<grid_for(n_threads, block_dim), block_dim, 0, as_stream(stream)>>>(
+      reinterpret_cast<gal_device_alloc *>(h->d_state), n_threads, rounds, seed, seg_every, seg_lo, seg_hi, d_classes,
+      d_stats);
+  GAL_CUDA_TRY(cudaGetLastError(), "mixed launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
+                                  uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,
+                                  uint32_t block_dim, uint64_t *h_stats, void *stream) {
+  if (h == nullptr || h_classes == nullptr || h_stats == nullptr) return fail_invalid("NULL argument");
+  const uint64_t bytes = n_threads * (uint64_t)rounds;
+  if (bytes > h->d_classes_bytes) {
+    if (h->d_classes) cudaFree(h->d_classes);
+    h->d_classes = nullptr;
+    h->d_classes_bytes = 0;
+    GAL_CUDA_TRY(cudaMalloc(&h->d_classes, bytes), "cudaMalloc class trace");
+    h->d_classes_bytes = bytes;
+  }
+  cudaStream_t s = as_stream(stream);
+  GAL_CUDA_TRY(cudaMemsetAsync(h->d_stats, 0, 64, s), "stats reset");
+  GAL_CUDA_TRY(cudaMemcpyAsync(h->d_classes, h_classes, bytes, cudaMemcpyHostToDevice, s), "trace H2D");
+  int rc = gal_run_mixed(h, n_threads, rounds, seed, seg_every, seg_lo, seg_hi, h->d_classes, block_dim,
+                         h->d_stats, stream);
+  if (rc != GAL_OK) return rc;
+  GAL_CUDA_TRY(cudaMemcpyAsync(h_stats, h->d_stats, 64, cudaMemcpyDeviceToHost, s), "stats D2H");
+  GAL_CUDA_TRY(cudaStreamSynchronize(s), "e2e sync");
+  return GAL_OK;
+}

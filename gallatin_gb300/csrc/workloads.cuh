@@ -1,0 +1,112 @@
+// Benchmark and test workloads over any allocator type with device
+// malloc(uint64_t) / free(void*) members.
+//
+// The same templates are instantiated over the GB300 allocator (capi_run.cu)
+// and over the reference's Gallatin<...> (oracle/ref_harness.cu), so both
+// sides of a comparison run identical kernels.
+//
+//   pairs  each thread: p = malloc(size); store tid; read it back; free(p)
+//          (the reference's per-thread correctness check,
+//          tests/src/gallatin_test.cu:58-112, fused into one kernel)
+//   mixed  each thread, for `rounds` rounds: size = 16 << class, where class
+//          is x mod 9 of a per-thread xorshift64 seeded by splitmix64(seed +
+//          tid) or read from a class trace; malloc, fill every 16 bytes with
+//          (tid ^ round), verify, free. Thread 0 of every seg_every-th CTA
+//          first makes one segment-tier request of a size drawn uniformly in
+//          [seg_lo, seg_hi] and touches its first and last 16 bytes.
+#ifndef GALLATIN_GB300_WORKLOADS_CUH
+#define GALLATIN_GB300_WORKLOADS_CUH
+
+#include <stdint.h>
+
+namespace galwork {
+
+enum { STAT_MISS = 0, STAT_BAD = 1, STAT_SEG_OK = 2, STAT_SEG_MISS = 3, STAT_WORDS = 8 };
+
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__host__ __device__ __forceinline__ uint64_t xorshift64(uint64_t &s) {
+  s ^= s << 13;
+  s ^= s >> 7;
+  s ^= s << 17;
+  return s;
+}
+
+// 16-byte load that the compiler cannot fold into the preceding stores.
+__device__ __forceinline__ ulonglong2 load_cg(const ulonglong2 *p) {
+  ulonglong2 v;
+  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+  return v;
+}
+
+template <class Alloc>
+__global__ void pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
+  const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  uint64_t *p = (uint64_t *)alloc->malloc(size);
+  if (p == nullptr) {
+    atomicAdd(stats + STAT_MISS, 1ull);
+    return;
+  }
+  p[0] = tid;
+  if (*(volatile uint64_t *)p != tid) atomicAdd(stats + STAT_BAD, 1ull);
+  alloc->free(p);
+}
+
+template <class Alloc>
+__global__ void mixed_kernel(Alloc *alloc, uint64_t n, uint32_t rounds, uint64_t seed, uint32_t seg_every,
+                             uint64_t seg_lo, uint64_t seg_hi, const uint8_t *classes,
+                             unsigned long long *stats) {
+  const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  if (tid >= n) return;
+  if (seg_every != 0 && threadIdx.x == 0 && blockIdx.x % seg_every == 0) {
+    const uint64_t j = blockIdx.x / seg_every;
+    const uint64_t size = seg_lo + splitmix64(seed + n + j) % (seg_hi - seg_lo + 1);
+    ulonglong2 *p = (ulonglong2 *)alloc->malloc(size);
+    if (p != nullptr) {
+      const uint64_t last = size / 16 - 1;
+      p[0] = make_ulonglong2(tid, j);
+      p[last] = make_ulonglong2(j, tid);
+      volatile unsigned long long *vp = (volatile unsigned long long *)p;
+      if (vp[0] != tid || vp[2 * last] != j) atomicAdd(stats + STAT_BAD, 1ull);
+      alloc->free(p);
+      atomicAdd(stats + STAT_SEG_OK, 1ull);
+    } else {
+      atomicAdd(stats + STAT_SEG_MISS, 1ull);
+    }
+  }
+  uint64_t s = splitmix64(seed + tid);
+  unsigned long long misses = 0, bad = 0;
+  for (uint32_t r = 0; r < rounds; ++r) {
+    const uint32_t cls = classes ? (uint32_t)classes[(uint64_t)r * n + tid] : (uint32_t)(xorshift64(s) % 9);
+    const uint64_t size = 16ull << cls;
+    ulonglong2 *p = (ulonglong2 *)alloc->malloc(size);
+    if (p == nullptr) {
+      ++misses;
+      continue;
+    }
+    const uint64_t v = tid ^ r;
+    const ulonglong2 fill = make_ulonglong2(v, v);
+    const uint64_t n16 = size / 16;
+    for (uint64_t i = 0; i < n16; ++i) p[i] = fill;
+    for (uint64_t i = 0; i < n16; ++i) {
+      const ulonglong2 got = load_cg(p + i);
+      if (got.x != v || got.y != v) {
+        ++bad;
+        break;
+      }
+    }
+    alloc->free(p);
+  }
+  if (misses) atomicAdd(stats + STAT_MISS, misses);
+  if (bad) atomicAdd(stats + STAT_BAD, bad);
+}
+
+}  // namespace galwork
+
+#endif  // GALLATIN_GB300_WORKLOADS_CUH

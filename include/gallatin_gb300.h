@@ -1,0 +1,180 @@
+/*
+ * gallatin_gb300 C ABI.
+ *
+ * Host entry points of the GB300 Gallatin allocator, behind plain C types:
+ * handles, pointers, sizes and a cudaStream_t passed as void*. No torch or
+ * C++ types cross this boundary. The device-side malloc/free that user
+ * kernels call are header-only (include/gallatin/allocators/gallatin.cuh);
+ * this library creates, inspects and destroys the state they operate on,
+ * and runs batch and benchmark kernels over it.
+ *
+ * Each entry names the reference interface it replaces (paths inside the
+ * saltsystemslab/gallatin tree). Calls on one handle are not thread-safe;
+ * different handles are independent. Every function returns GAL_OK or a
+ * GAL_ERR_* code; nothing here calls exit() or traps.
+ */
+#ifndef GALLATIN_GB300_H
+#define GALLATIN_GB300_H
+
+#include <stdint.h>
+
+#include "gallatin_gb300/state.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GAL_OK 0
+#define GAL_ERR_INVALID 1   /* bad argument or unsupported geometry */
+#define GAL_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define GAL_ERR_NOMEM 3     /* device or host allocation failed */
+
+typedef struct gal_allocator gal_allocator; /* opaque host handle */
+typedef struct gal_veb gal_veb;             /* opaque standalone vEB tree */
+
+typedef struct gal_geometry_t {
+  uint64_t segment_bytes;
+  uint64_t min_size;
+  uint64_t max_size;
+  uint64_t num_segments;
+  uint64_t arena_bytes;
+  uint32_t num_trees;
+  uint32_t blocks_per_segment;
+  uint32_t num_sms;
+  uint32_t total_slots;
+  uint32_t slot_count[GAL_MAX_TREES];
+  uint64_t arena_base; /* device address of the arena */
+} gal_geometry_t;
+
+typedef struct gal_stats_t {
+  uint64_t num_segments;
+  uint64_t free_segments;                    /* set leaf bits of the segment tree */
+  uint64_t tree_segments[GAL_MAX_TREES];     /* segments formatted for tree t */
+  uint64_t tree_blocks_out[GAL_MAX_TREES];   /* blocks of tree t not in a segment pool */
+  uint64_t tree_live_slices[GAL_MAX_TREES];  /* live count summed over those blocks */
+  uint64_t segment_allocations;              /* live multi-segment allocations */
+  uint64_t segments_in_allocations;          /* segments they span */
+  uint64_t counters[GAL_NUM_COUNTERS];
+} gal_stats_t;
+
+/* --- allocator lifetime (reference gallatin.cuh:324-421, :643-668) --- */
+
+/* Build an allocator over max_bytes / segment_bytes segments. segment_bytes,
+ * min_size and max_size must be powers of two with
+ * segment_bytes >= max_size * 4096 (reference static_assert gallatin.cuh:300)
+ * and max_size >= 32 * min_size (multi-slice runs fit one bitmap word).
+ * min_slots: floor on pinned blocks per size class (0 = default 8).
+ * Replaces Gallatin<seg,min,max>::generate_on_device. */
+int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size, uint64_t max_size,
+               uint32_t min_slots, gal_allocator **out);
+
+/* Free everything, arena included (reference free_on_device, gallatin.cuh:643). */
+int gal_destroy(gal_allocator *h);
+
+/* Device pointer to the allocator state: the value generate_on_device
+ * returns and user kernels receive (reference gallatin.cuh:419). */
+void *gal_device_state(gal_allocator *h);
+
+/* Handle owning a device state pointer, or NULL. Lets the header-only
+ * Gallatin<...> template map its device pointer back (reference
+ * free_on_device/print_info take the device pointer, gallatin.cuh:643,1855). */
+gal_allocator *gal_from_device_state(const void *device_state);
+
+int gal_geometry(gal_allocator *h, gal_geometry_t *out);
+
+/* --- stats (reference print_info gallatin.cuh:1855-1897,
+ *     report_fill veb.cuh:1052, print_global_stats global_allocator.cuh:86) --- */
+int gal_stats(gal_allocator *h, gal_stats_t *out);
+int gal_print_info(gal_allocator *h);
+int gal_reset_counters(gal_allocator *h);
+
+/* Copy one metadata array to host memory for invariant checks.
+ * which: see GAL_DUMP_*; tree selects the sub tree for GAL_DUMP_SUB_TREE
+ * and layer the vEB layer. gal_dump_bytes gives the size to provide. */
+#define GAL_DUMP_CHUNK_IDS 0
+#define GAL_DUMP_SEG_AVAIL 1
+#define GAL_DUMP_SEG_BLOCK_BITS 2
+#define GAL_DUMP_BLOCK_META 3
+#define GAL_DUMP_BLOCK_BITS 4
+#define GAL_DUMP_BLOCK_EXT 5
+#define GAL_DUMP_SLOTS 6
+#define GAL_DUMP_COUNTERS 7
+#define GAL_DUMP_SEGMENT_TREE 8
+#define GAL_DUMP_SUB_TREE 9
+#define GAL_DUMP_LOCKS 10
+int64_t gal_dump_bytes(gal_allocator *h, int which, int tree, int layer);
+int gal_dump(gal_allocator *h, int which, int tree, int layer, void *host_dst, uint64_t bytes);
+int gal_veb_layer_count(gal_allocator *h, int tree); /* tree -1 = segment tree */
+
+/* --- batch entry points (device buffers, one thread per request) ---
+ * These are the host-callable form of Gallatin::malloc / free
+ * (gallatin.cuh:1186,1378), as the reference tests drive them from
+ * kernels (tests/src/gallatin_test.cu:58-112). */
+int gal_malloc_batch(gal_allocator *h, const uint64_t *d_sizes, uint64_t n, uint64_t *d_ptrs, void *stream);
+int gal_free_batch(gal_allocator *h, const uint64_t *d_ptrs, uint64_t n, void *stream);
+
+/* Detach every pinned block (no malloc/free may run concurrently). Empty
+ * blocks and segments return to their pools, so after all allocations are
+ * freed the trees equal their initial state. No reference counterpart: the
+ * reference keeps its boot-time pinned blocks forever (gallatin.cuh:171). */
+int gal_flush_pinned(gal_allocator *h, void *stream);
+
+/* --- workloads over the device API (benchmarks and e2e) ---
+ * stats (device, 8 x u64): [0] slice/block misses (nullptr), [1] verify
+ * failures, [2] segment-tier successes, [3] segment-tier misses.
+ * Replaces the reference test kernels gallatin_test.cu:58-112 and
+ * gallatin_churn.cu:36-95 as benchmark drivers. */
+int gal_run_pairs(gal_allocator *h, uint64_t n_threads, uint64_t size, uint32_t block_dim,
+                  unsigned long long *d_stats, void *stream);
+int gal_run_mixed(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed, uint32_t seg_every,
+                  uint64_t seg_lo, uint64_t seg_hi, const uint8_t *d_classes, uint32_t block_dim,
+                  unsigned long long *d_stats, void *stream);
+/* Same workload end to end from host buffers: copies the class trace
+ * (rounds * n_threads bytes, round-major) to the device, runs, and copies
+ * the 8 stats words back, all on `stream`, then synchronises it. */
+int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed, uint32_t seg_every,
+                       uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes, uint32_t block_dim,
+                       uint64_t *h_stats, void *stream);
+
+/* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
+
+typedef struct gal_veb_op {
+  uint32_t code; /* GAL_VEB_OP_* */
+  uint32_t tid;  /* executing thread id (< 1024) for the hashed ops */
+  uint64_t arg;
+  uint64_t arg2;
+} gal_veb_op;
+
+#define GAL_VEB_OP_INSERT 0             /* insert(arg) -> bool           veb.cuh:757 */
+#define GAL_VEB_OP_INSERT_FORCE 1       /* insert_force_update(arg)      veb.cuh:775 */
+#define GAL_VEB_OP_REMOVE 2             /* remove(arg) -> bool           veb.cuh:737 */
+#define GAL_VEB_OP_QUERY 3              /* query(arg) -> bool            veb.cuh:824 */
+#define GAL_VEB_OP_SUCCESSOR 4          /* successor(arg) -> id|~0       veb.cuh:836 */
+#define GAL_VEB_OP_SUCCESSOR_THOROUGH 5 /* successor_thorough(arg)       veb.cuh:878 */
+#define GAL_VEB_OP_LOCK_OFFSET 6        /* lock_offset(arg)              veb.cuh:918 */
+#define GAL_VEB_OP_MALLOC_FIRST 7       /* malloc_first()                veb.cuh:979 */
+#define GAL_VEB_OP_FIND_FIRST 8         /* find_first_valid_index()      veb.cuh:940 */
+#define GAL_VEB_OP_FIND_RANDOM 9        /* find_random_valid_index()     veb.cuh:946 */
+#define GAL_VEB_OP_MALLOC 10            /* malloc()                      veb.cuh:993 */
+#define GAL_VEB_OP_GATHER 11            /* gather_multiple(arg)          veb.cuh:1160 */
+#define GAL_VEB_OP_RETURN 12            /* return_multiple(arg, arg2)    veb.cuh:1198 */
+#define GAL_VEB_OP_REPORT_FILL 13       /* set leaf bits                 veb.cuh:1052 */
+
+/* Full tree over [0, universe) (reference veb_tree::generate_on_device). */
+int gal_veb_create(uint64_t universe, uint64_t seed, gal_veb **out);
+int gal_veb_destroy(gal_veb *v);
+int gal_veb_num_layers(gal_veb *v);
+uint64_t gal_veb_layer_words(gal_veb *v, int layer);
+int gal_veb_dump(gal_veb *v, int layer, uint64_t *host_dst);
+/* Run ops in order on one 1024-thread block; op i runs on thread ops[i].tid
+ * and writes results[i]. d_ops/d_results are device buffers. */
+int gal_veb_run_ops(gal_veb *v, const gal_veb_op *d_ops, uint64_t n, uint64_t *d_results, void *stream);
+
+/* Last CUDA error text recorded by this library (static storage). */
+const char *gal_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GALLATIN_GB300_H */

@@ -1,0 +1,635 @@
+// Device allocator core: the three tiers of Gallatin's method on GB300.
+//
+//   slice tier    size <= max: a pinned block of the size's tree serves the
+//                 request; multi-slice runs of 2..64 slices for sizes up to
+//                 min*4096/2 (reference gallatin.cuh:1196-1217)
+//   block tier    up to segment size: a whole block (gallatin.cuh:828-861)
+//   segment tier  n contiguous segments (gallatin.cuh:790-826)
+//
+// The method is the reference's: segments tracked by vEB trees (the segment
+// tree hands out the smallest free id, sub trees pick a hashed random start),
+// segments formatted into power-of-two blocks of 4096 slices, a memory table
+// (chunk_ids) that maps a pointer back to its segment's tree on free.
+//
+// The GB300 design differs in how a block hands out slices. The reference
+// bumps a per-block counter and recycles a block only after all 4096 slices
+// came back (block.cuh:245-281). Here each block carries a 4096-bit slice
+// bitmap: a warp's same-class requests reserve capacity with one atomic on
+// the block's meta word (live count + cursor + tree/state tag), then claim
+// bits with fetch-and; frees return bits with fetch-or and release the
+// reservation. Freed slices are reused while the block stays pinned, so a
+// block is replaced only when it is full, and it is recycled to its
+// segment's free-block bitmap when its last slice comes back. Every wait is
+// bounded; exhausted budgets return nullptr and bump a device counter.
+#ifndef GALLATIN_GB300_ALLOC_CUH
+#define GALLATIN_GB300_ALLOC_CUH
+
+#include <stdint.h>
+
+#include "ptx.cuh"
+#include "state.h"
+#include "veb.cuh"
+
+namespace gal {
+
+constexpr int kSliceAttempts = 4096;      // group attempts per slice request
+constexpr int kClaimSteps = 160;          // fetch-and steps per reservation
+constexpr int kRequestBlockAttempts = 512;
+constexpr int kSegmentLockSpins = 1 << 20;
+constexpr int kSegmentLockBit = 31;
+
+enum { TIER_SLICE = 0, TIER_BLOCK = 1, TIER_SEGMENT = 2 };
+
+struct size_class {
+  int tier;
+  uint32_t tree;   // slice tree (slice tier) or block tree (block tier)
+  uint32_t count;  // slices per request (slice tier)
+  uint64_t nseg;   // segments (segment tier)
+};
+
+// Smallest e with 2^e >= v, for v >= 1 (reference get_first_bit_bigger,
+// alloc_utils.cuh:382-398).
+__host__ __device__ __forceinline__ int ceil_log2(uint64_t v) {
+#ifdef __CUDA_ARCH__
+  return 63 - __clzll((long long)v) + (__popcll(v) != 1);
+#else
+  return 63 - __builtin_clzll(v) + (__builtin_popcountll(v) != 1);
+#endif
+}
+
+// Size classing, identical to the reference's malloc dispatch
+// (gallatin.cuh:1141-1147, 1196-1260).
+__host__ __device__ __forceinline__ size_class classify(int min_shift, int num_trees, int block_shift_min,
+                                                        int segment_shift, uint64_t size) {
+  size_class sc;
+  sc.tier = TIER_SLICE;
+  sc.tree = 0;
+  sc.count = 1;
+  sc.nseg = 0;
+  if (size < (1ull << min_shift)) return sc;
+  const int cl = ceil_log2(size);
+  const int tree = cl - min_shift;
+  if (tree < num_trees) {
+    sc.tree = (uint32_t)tree;
+    return sc;
+  }
+  const int block_tree = cl - block_shift_min;
+  if (block_tree < 0) {
+    sc.tree = (uint32_t)(num_trees - 1);
+    sc.count = 1u << (tree - (num_trees - 1));
+    return sc;
+  }
+  if (block_tree < num_trees) {
+    sc.tier = TIER_BLOCK;
+    sc.tree = (uint32_t)block_tree;
+    return sc;
+  }
+  sc.tier = TIER_SEGMENT;
+  sc.nseg = ((size - 1) >> segment_shift) + 1;
+  return sc;
+}
+
+__device__ __forceinline__ size_class classify(const gal_state_t *st, uint64_t size) {
+  return classify(st->min_shift, st->num_trees, st->block_shift_min, st->segment_shift, size);
+}
+
+__device__ __forceinline__ uint32_t meta_live(uint64_t m) { return (uint32_t)m; }
+__device__ __forceinline__ uint32_t meta_tree(uint64_t m) { return (uint32_t)(m >> GAL_META_TREE_SHIFT) & 0xFFu; }
+__device__ __forceinline__ uint32_t meta_state(uint64_t m) { return (uint32_t)(m >> GAL_META_STATE_SHIFT) & 3u; }
+__device__ __forceinline__ uint32_t meta_cursor(uint64_t m) { return (uint32_t)(m >> GAL_META_CURSOR_SHIFT); }
+
+__device__ __forceinline__ void count(const gal_state_t *st, int id) {
+  atomicAdd(st->counters + id, 1ull);
+}
+
+__device__ __forceinline__ int block_index_shift(const gal_state_t *st) {
+  return st->segment_shift - st->block_shift_min;
+}
+
+__device__ __forceinline__ char *block_address(const gal_state_t *st, uint64_t b, uint32_t t) {
+  const int bis = block_index_shift(st);
+  const uint64_t seg = b >> bis;
+  const uint64_t i = b & ((1ull << bis) - 1);
+  return st->memory + (seg << st->segment_shift) + (i << (st->block_shift_min + (int)t));
+}
+
+__device__ __forceinline__ uint64_t *ext_words(const gal_state_t *st, uint64_t b) {
+  const int bis = block_index_shift(st);
+  const uint64_t seg = b >> bis;
+  const uint64_t i = b & ((1ull << bis) - 1);
+  return st->block_ext + ((seg * st->ext_blocks_per_segment + i) << 6);
+}
+
+// Aligned runs of c (a power of two <= 64) free bits: bit j is set when bits
+// j..j+c-1 are all set and j is a multiple of c.
+__device__ __forceinline__ uint64_t run_starts(uint64_t a, uint32_t c) {
+  if (c == 1) return a;
+  if (c >= 64) return (a == ~0ull) ? 1ull : 0ull;
+  uint64_t x = a;
+  for (uint32_t s = 1; s < c; s <<= 1) x &= x >> s;
+  return x & (~0ull / ((1ull << c) - 1));
+}
+
+__device__ __forceinline__ uint64_t expand_runs(uint64_t starts, uint32_t c) {
+  if (c >= 64) return starts ? ~0ull : 0ull;
+  return starts * ((1ull << c) - 1);
+}
+
+__device__ __forceinline__ uint64_t lowest_bits(uint64_t x, uint32_t k) {
+  uint64_t out = 0;
+  for (uint32_t i = 0; i < k && x; ++i) {
+    uint64_t low = x & (~x + 1);
+    out |= low;
+    x ^= low;
+  }
+  return out;
+}
+
+__device__ __forceinline__ void backoff(int attempt) {
+  int ns = 32 << ((attempt >> 4) < 5 ? (attempt >> 4) : 5);
+  __nanosleep(ns);
+}
+
+// ---- locks (bounded) -----------------------------------------------------
+
+__device__ __forceinline__ bool try_lock(const gal_state_t *st, int bit) {
+  return (atomicOr(st->locks, 1u << bit) & (1u << bit)) == 0;
+}
+
+__device__ __forceinline__ void unlock(const gal_state_t *st, int bit) {
+  __threadfence();
+  atomicAnd(st->locks, ~(1u << bit));
+}
+
+// ---- segments ------------------------------------------------------------
+
+__device__ inline void sub_tree_cleanup(const gal_state_t *st, uint32_t t, uint64_t seg) {
+  veb::remove(&st->sub_trees[t], seg);
+  if (ptx::ld_relaxed(st->chunk_ids + seg) == t && ptx::ld_relaxed(st->seg_avail + seg) > 0) {
+    veb::insert_force_update(&st->sub_trees[t], seg);
+  }
+}
+
+__device__ inline void try_retire_segment(const gal_state_t *st, uint64_t seg, uint32_t t, int32_t bps_t) {
+  if (ptx::cas_acq_rel(st->seg_avail + seg, bps_t, (int32_t)GAL_SEG_GATE) != bps_t) return;
+  veb::remove(&st->sub_trees[t], seg);
+  unsigned short prev = atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)t,
+                                  (unsigned short)GAL_FREE_SEGMENT);
+  if (prev != (unsigned short)t) count(st, GAL_CTR_CORRUPT);
+  __threadfence();
+  veb::insert_force_update(&st->segment_tree, seg);
+  count(st, GAL_CTR_SEGMENT_RETIRE);
+}
+
+// Add one free block to a segment's count and act on the transitions:
+// 0 -> 1 makes the segment findable again, all-free retires it.
+__device__ inline void seg_avail_add_one(const gal_state_t *st, uint64_t seg) {
+  const int32_t now = ptx::atom_add_release(st->seg_avail + seg, 1) + 1;
+  if (now <= 0) return;
+  const uint32_t t = ptx::ld_relaxed(st->chunk_ids + seg);
+  if (t >= (uint32_t)st->num_trees) return;
+  const int32_t bps_t = (int32_t)(st->blocks_per_segment >> t);
+  if (now == bps_t) {
+    try_retire_segment(st, seg, t, bps_t);
+  } else if (now == 1) {
+    veb::insert_force_update(&st->sub_trees[t], seg);
+  }
+}
+
+// Format the smallest free segment for tree t. Caller holds tree t's lock.
+__device__ inline uint64_t attach_segment(const gal_state_t *st, uint32_t t) {
+  const uint64_t seg = veb::malloc_first(&st->segment_tree);
+  if (seg == veb::kFail) return veb::kFail;
+  unsigned short prev = atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)GAL_FREE_SEGMENT,
+                                  (unsigned short)t);
+  if (prev != (unsigned short)GAL_FREE_SEGMENT) {
+    count(st, GAL_CTR_CORRUPT);
+    return veb::kFail;
+  }
+  const uint32_t bps_t = st->blocks_per_segment >> t;
+  uint64_t *words = st->seg_block_bits + seg * st->seg_block_words;
+  for (uint32_t w = 0; w < st->seg_block_words; ++w) {
+    const uint32_t lo = w * 64;
+    uint64_t v = 0;
+    if (bps_t >= lo + 64) v = ~0ull;
+    else if (bps_t > lo) v = (1ull << (bps_t - lo)) - 1;
+    ptx::st_relaxed(words + w, v);
+  }
+  ptx::atom_add_release(st->seg_avail + seg, (int32_t)bps_t - (int32_t)GAL_SEG_GATE);
+  veb::insert_force_update(&st->sub_trees[t], seg);
+  count(st, GAL_CTR_SEGMENT_ATTACH);
+  return seg;
+}
+
+// Take one free block out of segment `seg` (formatted for t). Returns its
+// global block id, exclusively owned and in state FREE, or GAL_EMPTY_BLOCK.
+__device__ inline uint32_t take_block(const gal_state_t *st, uint64_t seg, uint32_t t) {
+  const int32_t before = ptx::atom_add_acquire(st->seg_avail + seg, -1);
+  if (before <= 0) {
+    seg_avail_add_one(st, seg);
+    sub_tree_cleanup(st, t, seg);
+    return GAL_EMPTY_BLOCK;
+  }
+  if (ptx::ld_relaxed(st->chunk_ids + seg) != t) {
+    seg_avail_add_one(st, seg);
+    sub_tree_cleanup(st, t, seg);
+    return GAL_EMPTY_BLOCK;
+  }
+  if (before == 1) sub_tree_cleanup(st, t, seg);
+  uint64_t *words = st->seg_block_bits + seg * st->seg_block_words;
+  const int bis = block_index_shift(st);
+  for (int pass = 0; pass < 64; ++pass) {
+    for (uint32_t w = 0; w < st->seg_block_words; ++w) {
+      uint64_t v = ptx::ld_relaxed(words + w);
+      while (v) {
+        const uint64_t bit = v & (~v + 1);
+        const uint64_t old = ptx::atom_and_acquire(words + w, ~bit);
+        if (old & bit) return (uint32_t)((seg << bis) + w * 64 + (uint64_t)(__ffsll((long long)bit) - 1));
+        v = old & ~bit;
+      }
+    }
+  }
+  count(st, GAL_CTR_CORRUPT);
+  seg_avail_add_one(st, seg);
+  return GAL_EMPTY_BLOCK;
+}
+
+// Give a retired block back to its segment's free-block bitmap.
+__device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b) {
+  const int bis = block_index_shift(st);
+  const uint64_t seg = b >> bis;
+  const uint64_t i = b & ((1ull << bis) - 1);
+  ptx::red_or_relaxed(st->seg_block_bits + seg * st->seg_block_words + (i >> 6), 1ull << (i & 63));
+  seg_avail_add_one(st, seg);  // release add orders the bit before the count
+  count(st, GAL_CTR_BLOCK_RETIRE);
+}
+
+// A DETACHED block whose live count reached zero goes back to its segment.
+__device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
+  uint64_t *mp = st->block_meta + b;
+  uint64_t m = ptx::ld_relaxed(mp);
+  for (int i = 0; i < 64; ++i) {
+    if (meta_state(m) != GAL_STATE_DETACHED || meta_live(m) != 0) return;
+    const uint64_t nm = m - ((uint64_t)GAL_STATE_DETACHED << GAL_META_STATE_SHIFT);
+    const uint64_t r = ptx::cas_acq_rel(mp, m, nm);
+    if (r == m) {
+      return_block_to_segment(st, b);
+      return;
+    }
+    m = r;
+  }
+}
+
+__device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n) {
+  const uint64_t old = ptx::atom_add_release(st->block_meta + b, (uint64_t)(-(int64_t)n));
+  if (meta_state(old) == GAL_STATE_DETACHED && meta_live(old) == n) try_retire_block(st, b);
+}
+
+// Move a block this thread owns from FREE to `state` formatted for t,
+// adding `live` to its live count.
+__device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t state,
+                                          uint32_t live) {
+  const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
+  const int64_t dstate = (int64_t)state - (int64_t)meta_state(m);
+  const int64_t dtree = (int64_t)t - (int64_t)meta_tree(m);
+  const uint64_t delta = (uint64_t)(dstate * (1ll << GAL_META_STATE_SHIFT)) +
+                         (uint64_t)(dtree * (1ll << GAL_META_TREE_SHIFT)) + (uint64_t)live;
+  ptx::atom_add_release(st->block_meta + b, delta);
+}
+
+__device__ __forceinline__ uint64_t mix_tid(uint64_t tid, int attempt) {
+  return attempt == 0 ? tid : murmur64a_u64(tid, (uint64_t)attempt);
+}
+
+// A FREE block of tree t, from a segment already formatted for t or from a
+// newly attached one. GAL_EMPTY_BLOCK when the arena cannot provide one.
+__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint64_t tid) {
+  const gal_veb_t *sub = &st->sub_trees[t];
+  for (int a = 0; a < kRequestBlockAttempts; ++a) {
+    uint64_t seg = veb::find_random_valid_index(sub, mix_tid(tid, a));
+    if (seg == veb::kFail) {
+      if (try_lock(st, (int)t)) {
+        seg = attach_segment(st, t);
+        unlock(st, (int)t);
+        if (seg == veb::kFail) {
+          if (veb::find_first_valid_index(sub) == veb::kFail) return GAL_EMPTY_BLOCK;
+          continue;
+        }
+      } else {
+        backoff(a);
+        continue;
+      }
+    }
+    const uint32_t b = take_block(st, seg, t);
+    if (b != GAL_EMPTY_BLOCK) return b;
+  }
+  count(st, GAL_CTR_TIMEOUT);
+  return GAL_EMPTY_BLOCK;
+}
+
+// ---- pinned blocks -------------------------------------------------------
+
+__device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t) {
+  ulonglong2 *bits = reinterpret_cast<ulonglong2 *>(st->block_bits + (b << 6));
+  const ulonglong2 ones = make_ulonglong2(~0ull, ~0ull);
+  for (int i = 0; i < 32; ++i) bits[i] = ones;
+  if (t == (uint32_t)st->num_trees - 1) {
+    ulonglong2 *ext = reinterpret_cast<ulonglong2 *>(ext_words(st, b));
+    const ulonglong2 zero = make_ulonglong2(0ull, 0ull);
+    for (int i = 0; i < 32; ++i) ext[i] = zero;
+  }
+  own_block(st, b, t, GAL_STATE_PINNED, 0);  // release: bitmap before PINNED
+  count(st, GAL_CTR_BLOCK_PINS);
+}
+
+__device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) {
+  const uint64_t old = ptx::atom_add_release(
+      st->block_meta + b, (uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
+  if (meta_live(old) == 0) try_retire_block(st, b);
+}
+
+// Replace the block a slot holds (`seen`, without the REPLACING flag) by a
+// freshly pinned one. Only the thread whose CAS sets REPLACING does the work.
+__device__ inline uint32_t replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t,
+                                        uint64_t tid) {
+  if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return GAL_EMPTY_BLOCK;
+  const uint32_t nb = request_block(st, t, tid);
+  if (nb == GAL_EMPTY_BLOCK) {
+    ptx::st_release(slot, seen);
+    return GAL_EMPTY_BLOCK;
+  }
+  pin_block(st, nb, t);
+  ptx::st_release(slot, (uint64_t)nb);
+  if ((uint32_t)seen != GAL_EMPTY_BLOCK) detach_block(st, (uint32_t)seen);
+  return nb;
+}
+
+// ---- slice tier ----------------------------------------------------------
+
+// Warp-aggregated slice allocation. Lanes asking for the same (tree, count)
+// form one group; its leader reserves the group's total with one atomic on
+// the pinned block's meta word and claims bits with fetch-and.
+__device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t c, uint64_t tid) {
+  const uint32_t active = __activemask();
+  const uint32_t key = (t << 8) | (uint32_t)(__ffs((int)c) - 1);
+  const uint32_t peers = __match_any_sync(active, key);
+  const uint32_t lane = ptx::laneid();
+  const uint32_t lt = ptx::lanemask_lt();
+  const uint32_t nslots = st->slot_count[t];
+  const uint32_t slot0 = ptx::smid() % nslots;
+  uint64_t *const slots = st->slots + st->slot_offset[t];
+  const uint32_t ext_tree = (uint32_t)st->num_trees - 1;
+  void *result = nullptr;
+  bool done = false;
+  for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
+    const uint32_t grp = __ballot_sync(peers, !done);
+    if (grp == 0) break;
+    if (done) continue;
+    const int leader = __ffs((int)grp) - 1;
+    const uint32_t g_n = __popc(grp);
+    const uint32_t g_rank = __popc(grp & lt);
+    const uint32_t need = g_n * c;
+    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3)) % nslots;
+
+    uint32_t b = GAL_EMPTY_BLOCK;
+    uint32_t cursor = 0;
+    uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
+    if (lane == (uint32_t)leader) {
+      const uint64_t sv = ptx::ld_acquire(slot);
+      if (sv & GAL_SLOT_REPLACING) {
+        backoff(attempt);
+      } else {
+        b = (uint32_t)sv;
+        if (b == GAL_EMPTY_BLOCK) b = replace_slot(st, slot, sv, t, tid);
+        if (b != GAL_EMPTY_BLOCK) {
+          uint64_t m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)need << GAL_META_CURSOR_SHIFT) | need);
+          take = g_n;
+          if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED) {
+            release_live(st, b, need);
+            take = 0;
+          } else if (meta_live(m) + need > GAL_BLOCK_SLICES) {
+            // full for the whole group: undo, then reserve what still fits
+            release_live(st, b, need);
+            const uint32_t room = meta_live(m) < GAL_BLOCK_SLICES ? GAL_BLOCK_SLICES - meta_live(m) : 0;
+            take = room / c < g_n ? room / c : g_n;
+            if (take > 0) {
+              const uint32_t part = take * c;
+              m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)part << GAL_META_CURSOR_SHIFT) | part);
+              if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED ||
+                  meta_live(m) + part > GAL_BLOCK_SLICES) {
+                release_live(st, b, part);
+                take = 0;
+              }
+            }
+            if (take == 0) replace_slot(st, slot, (uint64_t)b, t, tid);
+          }
+          if (take > 0) {
+            cursor = meta_cursor(m) & (GAL_BLOCK_SLICES - 1);
+          } else {
+            b = GAL_EMPTY_BLOCK;
+          }
+        } else {
+          backoff(attempt);
+        }
+      }
+    }
+    b = __shfl_sync(grp, b, leader);
+    if (b == GAL_EMPTY_BLOCK) continue;
+    take = __shfl_sync(grp, take, leader);
+
+    uint64_t *const bits = st->block_bits + ((uint64_t)b << 6);
+    int my_slice = -1;
+    uint32_t acc = 0;
+    // leader-private search state: word, and what is known free in it
+    uint32_t w = cursor >> 6;
+    uint32_t lo = ((cursor & 63) + c - 1) & ~(c - 1);
+    uint64_t avail = lo >= 64 ? 0ull : (~0ull << lo);
+    for (int step = 0; step < kClaimSteps && acc < take; ++step) {
+      uint64_t got = 0;
+      uint32_t gw = w;
+      if (lane == (uint32_t)leader) {
+        const uint64_t pick = lowest_bits(run_starts(avail, c), take - acc);
+        if (pick) {
+          const uint64_t mask = expand_runs(pick, c);
+          const uint64_t old = ptx::atom_and_acquire(bits + w, ~mask);
+          const uint64_t gotbits = old & mask;
+          got = run_starts(gotbits, c) & pick;
+          const uint64_t partial = gotbits & ~expand_runs(got, c);
+          if (partial) ptx::red_or_relaxed(bits + w, partial);
+          if (c > 1 && got) ptx::red_or_relaxed(ext_words(st, b) + w, expand_runs(got, c) & ~got);
+          avail = old & ~mask;
+        } else {
+          avail = 0;
+        }
+        if (run_starts(avail, c) == 0) {
+          w = (w + 1) & 63;
+          avail = ~0ull;
+        }
+      }
+      got = ptx::shfl64(grp, got, leader);
+      gw = __shfl_sync(grp, gw, leader);
+      const uint32_t k = (uint32_t)__popcll(got);
+      if (g_rank >= acc && g_rank < acc + k) my_slice = (int)(gw * 64 + (uint32_t)ptx::nth_set_bit(got, (int)(g_rank - acc)));
+      acc += k;
+    }
+    if (acc < take && lane == (uint32_t)leader) {
+      release_live(st, b, (take - acc) * c);
+      // a reservation that found no aligned run: the block is too fragmented
+      // for this run length, so give the slot a fresh block
+      if (c > 1) replace_slot(st, slot, (uint64_t)b, t, tid);
+    }
+    if (my_slice >= 0) {
+      result = block_address(st, b, t) + ((uint64_t)my_slice << (st->min_shift + (int)t));
+      done = true;
+    }
+  }
+  if (!done) count(st, GAL_CTR_OOM_SLICE);
+  (void)ext_tree;
+  return result;
+}
+
+// Warp-aggregated slice free: one fetch-or per (block, word) and one
+// release of the live count per block.
+__device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t t, uint64_t off_s) {
+  const uint32_t active = __activemask();
+  const int bis = block_index_shift(st);
+  const uint64_t i = off_s >> (st->block_shift_min + (int)t);
+  const uint64_t b = (seg << bis) + i;
+  const uint32_t slice = (uint32_t)(off_s >> (st->min_shift + (int)t)) & (GAL_BLOCK_SLICES - 1);
+  const uint32_t word = slice >> 6;
+  const uint32_t bit = slice & 63;
+  uint32_t c = 1;
+  uint64_t *extw = nullptr;
+  if (t == (uint32_t)st->num_trees - 1) {
+    extw = ext_words(st, b) + word;
+    const uint64_t e = ptx::ld_relaxed(extw);
+    if (bit < 63) c = (uint32_t)__ffsll((long long)~(e >> (bit + 1)));
+  }
+  const uint64_t mask = ((c >= 64) ? ~0ull : ((1ull << c) - 1)) << bit;
+  const uint64_t cont = mask & ~(1ull << bit);
+  const uint32_t lane = ptx::laneid();
+
+  const uint32_t wpeers = __match_any_sync(active, (unsigned long long)((b << 6) | word));
+  const uint64_t or_mask = ptx::reduce_or64(wpeers, mask);
+  const uint64_t ext_mask = ptx::reduce_or64(wpeers, cont);
+  __syncwarp(active);  // every lane's payload writes before the release below
+  if (lane == (uint32_t)(__ffs((int)wpeers) - 1)) {
+    if (ext_mask) ptx::red_and_relaxed(extw, ~ext_mask);
+    ptx::red_or_release(st->block_bits + (b << 6) + word, or_mask);
+  }
+  const uint32_t bpeers = __match_any_sync(active, (unsigned long long)b);
+  const uint32_t total = __reduce_add_sync(bpeers, c);
+  __syncwarp(active);  // bitmap returns before the live count drops
+  if (lane == (uint32_t)(__ffs((int)bpeers) - 1)) release_live(st, b, total);
+}
+
+// ---- block and segment tiers ---------------------------------------------
+
+__device__ inline void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_t tid) {
+  const uint32_t b = request_block(st, bt, tid);
+  if (b == GAL_EMPTY_BLOCK) {
+    count(st, GAL_CTR_OOM_BLOCK);
+    return nullptr;
+  }
+  own_block(st, b, bt, GAL_STATE_DETACHED, 1);
+  return block_address(st, b, bt);
+}
+
+__device__ inline void *malloc_segment(const gal_state_t *st, uint64_t nseg) {
+  const uint64_t max_n = 0xFFFEull - (uint64_t)st->num_trees - 1;
+  if (nseg > st->num_segments || nseg > max_n) {
+    count(st, GAL_CTR_OOM_SEGMENT);
+    return nullptr;
+  }
+  int spins = 0;
+  while (!try_lock(st, kSegmentLockBit)) {
+    if (++spins >= kSegmentLockSpins) {
+      count(st, GAL_CTR_TIMEOUT);
+      return nullptr;
+    }
+    backoff(spins);
+  }
+  const uint64_t first = veb::gather_run(&st->segment_tree, nseg);
+  unlock(st, kSegmentLockBit);
+  if (first == veb::kFail) {
+    count(st, GAL_CTR_OOM_SEGMENT);
+    return nullptr;
+  }
+  const unsigned short tag = (unsigned short)((uint64_t)st->num_trees + 1 + nseg);
+  if (atomicCAS((unsigned short *)(st->chunk_ids + first), (unsigned short)GAL_FREE_SEGMENT, tag) !=
+      (unsigned short)GAL_FREE_SEGMENT) {
+    count(st, GAL_CTR_CORRUPT);
+    return nullptr;
+  }
+  return st->memory + (first << st->segment_shift);
+}
+
+__device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_t id) {
+  const uint64_t n = (uint64_t)id - (uint64_t)st->num_trees - 1;
+  if (atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)id, (unsigned short)GAL_FREE_SEGMENT) !=
+      (unsigned short)id) {
+    count(st, GAL_CTR_BAD_FREE);
+    return;
+  }
+  __threadfence();
+  veb::return_run(&st->segment_tree, seg, n);
+}
+
+// ---- public entry points -------------------------------------------------
+
+__device__ inline void *malloc(const gal_state_t *st, uint64_t size) {
+  const size_class sc = classify(st, size);
+  const uint64_t tid = veb::thread_tid();
+  if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, sc.count, tid);
+  if (sc.tier == TIER_BLOCK) return malloc_block(st, sc.tree, tid);
+  return malloc_segment(st, sc.nseg);
+}
+
+__device__ inline void free(const gal_state_t *st, void *ptr) {
+  if (ptr == nullptr) return;
+  const uint64_t off = (uint64_t)((char *)ptr - st->memory);
+  if (off >= st->arena_bytes) {
+    count(st, GAL_CTR_BAD_FREE);
+    return;
+  }
+  const uint64_t seg = off >> st->segment_shift;
+  const uint16_t id = ptx::ld_relaxed(st->chunk_ids + seg);
+  if (id < (uint16_t)st->num_trees) {
+    free_slice(st, seg, id, off & (st->segment_bytes - 1));
+  } else if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees) {
+    free_segment(st, seg, id);
+  } else {
+    count(st, GAL_CTR_BAD_FREE);
+  }
+}
+
+// Bytes a request of `size` really occupies (reference get_allocated_size,
+// gallatin.cuh:1152-1183, whose tier test compares against num_trees the
+// same way).
+__device__ inline uint64_t allocated_size(const gal_state_t *st, uint64_t size) {
+  if (size < 16) size = 16;
+  const int bit_size = ceil_log2(size);
+  const int tree = (size < (1ull << st->min_shift)) ? 0 : bit_size - st->min_shift;
+  if (tree > st->num_trees) {
+    const int block_tree = bit_size - st->block_shift_min;
+    if (block_tree > st->num_trees) return (((size - 1) >> st->segment_shift) + 1) << st->segment_shift;
+  }
+  return 1ull << bit_size;
+}
+
+__device__ __forceinline__ bool owns_allocation(const gal_state_t *st, const void *ptr) {
+  return (uint64_t)((const char *)ptr - st->memory) < st->arena_bytes;
+}
+
+// Detach the block a slot holds (maintenance; no mallocs may run).
+__device__ inline void flush_slot(const gal_state_t *st, uint64_t *slot) {
+  const uint64_t sv = ptx::ld_relaxed(slot);
+  const uint32_t b = (uint32_t)sv;
+  if (b == GAL_EMPTY_BLOCK || (sv & GAL_SLOT_REPLACING)) return;
+  if (atomicCAS((unsigned long long *)slot, sv, (unsigned long long)GAL_EMPTY_BLOCK) != sv) return;
+  detach_block(st, b);
+}
+
+}  // namespace gal
+
+#endif  // GALLATIN_GB300_ALLOC_CUH

@@ -1,0 +1,216 @@
+"""ORACLE — test infrastructure only.
+
+Bindings to the CPU restatement of the reference vEB tree (veb_oracle.c), the
+glibc CPU-baseline replay (cpu_replay.c) and, when it has been built, the
+reference's own CUDA build (oracle/_ref/libgalref.so, from ref_harness.cu).
+Only tests/, the smoke check and bench.py's baseline legs use this package;
+the product (gallatin_gb300/) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_int, c_int64, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+from . import build
+
+VEB_OP_DTYPE = np.dtype([("code", "<u4"), ("tid", "<u4"), ("arg", "<u8"), ("arg2", "<u8")])
+FAIL = (1 << 64) - 1
+MODE_REFERENCE = 0
+MODE_GB300 = 1
+
+_ORACLE = None
+_REPLAY = None
+_REF = None
+
+
+def load_oracle():
+    global _ORACLE
+    if _ORACLE is None:
+        build.build_oracle()
+        lib = ctypes.CDLL(str(build.oracle_lib()))
+        lib.oracle_veb_shape.restype = c_int
+        lib.oracle_veb_shape.argtypes = [c_uint64, c_void_p]
+        lib.oracle_veb_run.restype = c_int64
+        lib.oracle_veb_run.argtypes = [c_uint64, c_uint64, c_int, c_void_p, c_uint64, c_void_p, c_void_p, c_void_p]
+        lib.oracle_murmur64a_u64.restype = c_uint64
+        lib.oracle_murmur64a_u64.argtypes = [c_uint64, c_uint64]
+        _ORACLE = lib
+    return _ORACLE
+
+
+def veb_shape(universe: int) -> list[int]:
+    words = np.zeros(8, dtype=np.uint64)
+    layers = load_oracle().oracle_veb_shape(universe, words.ctypes.data)
+    if layers < 0:
+        raise ValueError(f"bad universe {universe}")
+    return [int(w) for w in words[:layers]]
+
+
+def veb_run(universe: int, seed: int, mode: int, ops: np.ndarray):
+    """Run ops on a full tree. Returns (results, layers top-first, quirks-so-far per op)."""
+    ops = np.ascontiguousarray(ops, dtype=VEB_OP_DTYPE)
+    n = len(ops)
+    results = np.zeros(n, dtype=np.uint64)
+    quirks = np.zeros(n, dtype=np.uint64)
+    shape = veb_shape(universe)
+    flat = np.zeros(sum(shape), dtype=np.uint64)
+    rc = load_oracle().oracle_veb_run(
+        universe, seed, mode, ops.ctypes.data, n, results.ctypes.data, flat.ctypes.data, quirks.ctypes.data
+    )
+    if rc < 0:
+        raise ValueError("oracle rejected the arguments")
+    layers, off = [], 0
+    for w in shape:
+        layers.append(flat[off : off + w].copy())
+        off += w
+    return results, layers, quirks
+
+
+def murmur64a(key: int, seed: int) -> int:
+    return int(load_oracle().oracle_murmur64a_u64(key, seed))
+
+
+# -- glibc CPU baseline --------------------------------------------------------
+def load_replay():
+    global _REPLAY
+    if _REPLAY is None:
+        build.build_oracle()
+        lib = ctypes.CDLL(str(build.replay_lib()))
+        lib.cpu_replay_mixed.restype = c_double
+        lib.cpu_replay_mixed.argtypes = [
+            c_uint64, c_uint64, c_uint64, c_uint32, c_uint64, c_void_p, c_uint32, c_uint32, c_uint64, c_uint64,
+            c_int, POINTER(c_uint64), POINTER(c_uint64),
+        ]
+        lib.cpu_replay_pairs.restype = c_double
+        lib.cpu_replay_pairs.argtypes = [c_uint64, c_uint64, c_int, POINTER(c_uint64), POINTER(c_uint64)]
+        lib.cpu_mixed_classes.restype = None
+        lib.cpu_mixed_classes.argtypes = [c_uint64, c_uint32, c_uint64, c_void_p]
+        _REPLAY = lib
+    return _REPLAY
+
+
+def cpu_mixed_classes(n: int, rounds: int, seed: int) -> np.ndarray:
+    out = np.empty(n * rounds, dtype=np.uint8)
+    load_replay().cpu_mixed_classes(n, rounds, seed, out.ctypes.data)
+    return out.reshape(rounds, n)
+
+
+def cpu_replay_mixed(n, tid_begin, tid_end, rounds, seed, *, seg_every=0, block_dim=256, seg_lo=16 << 20,
+                     seg_hi=256 << 20, workers=1, classes: np.ndarray | None = None):
+    misses, bad = c_uint64(0), c_uint64(0)
+    ptr = classes.ctypes.data if classes is not None else None
+    secs = load_replay().cpu_replay_mixed(n, tid_begin, tid_end, rounds, seed, ptr, seg_every, block_dim, seg_lo,
+                                          seg_hi, workers, ctypes.byref(misses), ctypes.byref(bad))
+    return secs, misses.value, bad.value
+
+
+def cpu_replay_pairs(n, size, workers=1):
+    misses, bad = c_uint64(0), c_uint64(0)
+    secs = load_replay().cpu_replay_pairs(n, size, workers, ctypes.byref(misses), ctypes.byref(bad))
+    return secs, misses.value, bad.value
+
+
+# -- the reference's own CUDA build -------------------------------------------
+def load_ref(build_if_missing: bool = True):
+    """ctypes handle of oracle/_ref/libgalref.so, or None when unavailable."""
+    global _REF
+    if _REF is not None:
+        return _REF
+    if build_if_missing and not build.ref_lib().exists():
+        try:
+            build.build_reference()
+        except RuntimeError:
+            return None
+    if not build.ref_lib().exists():
+        return None
+    lib = ctypes.CDLL(str(build.ref_lib()))
+    vp, u64, u32, i32 = c_void_p, c_uint64, c_uint32, c_int
+    sigs = {
+        "galref_veb_create": (i32, [u64, u64, POINTER(vp)]),
+        "galref_veb_destroy": (i32, [vp]),
+        "galref_veb_num_layers": (i32, [vp]),
+        "galref_veb_layer_words": (u64, [vp, i32]),
+        "galref_veb_dump": (i32, [vp, i32, vp]),
+        "galref_veb_run_ops": (i32, [vp, vp, u64, vp, vp]),
+        "galref_create": (i32, [u64, u64, u64, u64, u64, POINTER(vp)]),
+        "galref_destroy": (i32, [vp]),
+        "galref_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
+        "galref_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "galref_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _REF = lib
+    return lib
+
+
+class RefVeb:
+    """The reference veb_tree on the GPU (generate_on_device: full tree)."""
+
+    def __init__(self, universe: int, seed: int):
+        lib = load_ref()
+        if lib is None:
+            raise RuntimeError("reference build unavailable")
+        h = c_void_p()
+        if lib.galref_veb_create(universe, seed, ctypes.byref(h)) != 0:
+            raise RuntimeError("galref_veb_create failed")
+        self._lib, self._h = lib, h.value
+
+    def run_ops(self, d_ops: int, n: int, d_results: int, stream: int = 0) -> None:
+        if self._lib.galref_veb_run_ops(self._h, d_ops, n, d_results, stream) != 0:
+            raise RuntimeError("galref_veb_run_ops failed")
+
+    def layers(self) -> list[np.ndarray]:
+        out = []
+        for layer in range(self._lib.galref_veb_num_layers(self._h)):
+            arr = np.empty(self._lib.galref_veb_layer_words(self._h, layer), dtype=np.uint64)
+            if self._lib.galref_veb_dump(self._h, layer, arr.ctypes.data) != 0:
+                raise RuntimeError("galref_veb_dump failed")
+            out.append(arr)
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.galref_veb_destroy(self._h)
+            self._h = None
+
+
+class RefGallatin:
+    """The reference Gallatin<seg,min,max> on the GPU behind the shared workloads."""
+
+    def __init__(self, max_bytes: int, seed: int, segment_size=16 << 20, min_size=16, max_size=4096):
+        lib = load_ref()
+        if lib is None:
+            raise RuntimeError("reference build unavailable")
+        h = c_void_p()
+        rc = lib.galref_create(max_bytes, seed, segment_size, min_size, max_size, ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"galref_create failed ({rc})")
+        self._lib, self._h = lib, h.value
+
+    def run_pairs(self, n, size, d_stats, block_dim=1024, stream=0):
+        if self._lib.galref_run_pairs(self._h, n, size, block_dim, d_stats, stream) != 0:
+            raise RuntimeError("galref_run_pairs failed")
+
+    def run_mixed(self, n, rounds, seed, d_stats, *, seg_every=0, seg_lo=16 << 20, seg_hi=256 << 20, d_classes=0,
+                  block_dim=256, stream=0):
+        if self._lib.galref_run_mixed(self._h, n, rounds, seed, seg_every, seg_lo, seg_hi, d_classes, block_dim,
+                                      d_stats, stream) != 0:
+            raise RuntimeError("galref_run_mixed failed")
+
+    def run_mixed_host(self, n, rounds, seed, h_classes_ptr, *, seg_every=0, seg_lo=16 << 20, seg_hi=256 << 20,
+                       block_dim=256, stream=0):
+        out = np.zeros(8, dtype=np.uint64)
+        if self._lib.galref_run_mixed_host(self._h, n, rounds, seed, seg_every, seg_lo, seg_hi, h_classes_ptr,
+                                           block_dim, out.ctypes.data, stream) != 0:
+            raise RuntimeError("galref_run_mixed_host failed")
+        return out
+
+    def close(self):
+        if self._h:
+            self._lib.galref_destroy(self._h)
+            self._h = None

@@ -1,0 +1,51 @@
+"""The C-ABI library loads and exports every entry point gallatin_gb300.h declares (no GPU needed)."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+import pytest
+
+from conftest import REPO
+
+
+def declared_functions() -> list[str]:
+    text = (REPO / "include" / "gallatin_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(gal_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for expected in ("gal_create", "gal_destroy", "gal_malloc_batch", "gal_free_batch", "gal_veb_run_ops"):
+        assert expected in names
+    assert len(names) >= 24
+
+
+def test_library_exports_every_declared_symbol():
+    from gallatin_gb300 import _build
+
+    lib_file = _build.build()
+    lib = ctypes.CDLL(str(lib_file))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+
+
+def test_package_binds_without_gpu():
+    import gallatin_gb300 as gal
+
+    lib = gal.load()
+    assert lib.gal_last_error() is not None
+
+
+def test_invalid_geometry_is_rejected_without_touching_the_gpu():
+    import gallatin_gb300 as gal
+
+    # validation happens before any CUDA call
+    with pytest.raises(gal.GalError, match="power"):
+        gal.Gallatin.generate_on_device(1 << 30, 1, print_info=False, segment_size=3 << 20)
+    with pytest.raises(gal.GalError, match="max_size"):
+        gal.Gallatin.generate_on_device(1 << 30, 1, print_info=False, min_size=64, max_size=1024)
+    with pytest.raises(gal.GalError, match="segment"):
+        gal.Gallatin.generate_on_device(1 << 30, 1, print_info=False, segment_size=1 << 20, max_size=4096)
