@@ -45,6 +45,12 @@ WORKLOADS = {
         seg_every=64, seg_lo=16 * MIB, seg_hi=256 * MIB,
     ),
     "pairs": dict(arena=2 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=1_048_576, size=16, block=1024),
+    # the mixed workload without its 256 segment-tier requests: only the
+    # slice tier runs, which is what the reference arm can be compared on
+    "mixed-slices": dict(
+        arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=4_194_304, rounds=8, block=256,
+        seg_every=0, seg_lo=16 * MIB, seg_hi=256 * MIB,
+    ),
 }
 
 
@@ -165,13 +171,13 @@ def cpu_baseline(name: str, w: dict) -> dict:
     import oracle
 
     cores = os.cpu_count() or 1
-    if name == "mixed":
+    if name in ("mixed", "mixed-slices"):
         n, rounds = w["threads"], w["rounds"]
         secs, misses, bad = oracle.cpu_replay_mixed(
             n, 0, n, rounds, 42, seg_every=w["seg_every"], block_dim=w["block"], seg_lo=w["seg_lo"],
             seg_hi=w["seg_hi"], workers=cores,
         )
-        units = n * rounds + n // w["block"] // w["seg_every"]
+        units = n * rounds + (n // w["block"] // w["seg_every"] if w["seg_every"] else 0)
         sample = f"full workload: {n} threads x {rounds} rounds + segment-tier requests, glibc malloc/free"
     else:
         n = w["threads"]
@@ -201,11 +207,32 @@ def run(args) -> dict | None:
         dist.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.threads:
+        w["threads"] = args.threads
+    if args.rounds and "rounds" in w:
+        w["rounds"] = args.rounds
+    if args.arena_gib:
+        w["arena"] = int(args.arena_gib * GIB)
     impl = args.impl
     if impl == "reference":
         import oracle
 
+        if args.workload == "mixed":
+            # Not run again: on this workload the reference's CUDA build trapped
+            # (cudaErrorLaunchFailure, Xid 43). A segment-tier free puts its
+            # segments back in the segment tree before it resets their
+            # memory-table tag (reference gallatin.cuh:1283-1302), so a
+            # concurrent attach or gather finds the old tag in set_tree_id and
+            # executes `trap` (gallatin.cuh:802-811, 1477-1489).
+            if rank == 0:
+                print(json.dumps({
+                    "impl": "reference",
+                    "unavailable": "the reference CUDA build trapped on this workload (segment-tier free returns "
+                                   "segments before resetting their tag, gallatin.cuh:1283-1302; a concurrent attach "
+                                   "traps in set_tree_id, gallatin.cuh:1477-1489); not run again",
+                }))
+            return None
         if oracle.load_ref() is None:
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "reference CUDA build (oracle/_ref) is not built"}))
@@ -221,14 +248,14 @@ def run(args) -> dict | None:
     stats = torch.zeros(8, dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * MIB, dtype=torch.uint8, device="cuda")
 
-    if args.workload == "mixed":
+    if args.workload in ("mixed", "mixed-slices"):
         from gallatin_gb300.workload import mixed_class_trace, mixed_mean_bytes
 
         n, rounds = w["threads"], w["rounds"]
         trace = mixed_class_trace(n, rounds, 42)
         d_trace = torch.from_numpy(trace.reshape(-1)).cuda()
         h_trace = torch.from_numpy(trace.reshape(-1)).pin_memory()
-        seg_requests = n // w["block"] // w["seg_every"]
+        seg_requests = n // w["block"] // w["seg_every"] if w["seg_every"] else 0
         units = n * rounds + seg_requests
         alg_bytes = n * rounds * 2 * mixed_mean_bytes() + seg_requests * 64
 
@@ -359,7 +386,9 @@ def run(args) -> dict | None:
         "step_ms": times,
     }
     if impl == "gb300":
-        result["allocator_counters"] = a.stats()["counters"]
+        st_all = a.stats()
+        result["allocator_counters"] = st_all["counters"]
+        result["tree_pins"] = st_all["tree_pins"]
     close_allocator(impl, a)
     if rank == 0 and impl == "gb300" and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, w)
@@ -384,6 +413,9 @@ def main() -> int:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--threads", type=int, default=0, help="override the thread count (small profiling cases)")
+    ap.add_argument("--rounds", type=int, default=0, help="override the rounds of the mixed workload")
+    ap.add_argument("--arena-gib", type=float, default=0.0, help="override the arena size")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     res = run(args)

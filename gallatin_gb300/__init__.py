@@ -41,7 +41,7 @@ __all__ = [
 ]
 
 GAL_MAX_TREES = 24
-GAL_NUM_COUNTERS = 16
+GAL_NUM_COUNTERS = 64
 GAL_EMPTY_BLOCK = 0xFFFFFFFF
 GAL_FREE_SEGMENT = 0xFFFF
 GAL_SEG_GATE = -(1 << 28)
@@ -75,6 +75,7 @@ DUMP = {
     "segment_tree": (8, np.uint64),
     "sub_tree": (9, np.uint64),
     "locks": (10, np.uint32),
+    "adopt_tree": (11, np.uint64),
 }
 
 COUNTERS = [
@@ -88,7 +89,16 @@ COUNTERS = [
     "segment_attach",
     "segment_retire",
     "block_retire",
+    "replace_empty",
+    "replace_full",
+    "replace_frag",
+    "claim_short",
+    "stale_slot",
+    "slot_busy",
+    "replace_refill",
+    "adopt",
 ]
+TREE_PIN_COUNTER = 32
 
 
 class GalError(RuntimeError):
@@ -138,7 +148,9 @@ def load(path: str | Path | None = None):
     global _LIB
     if _LIB is not None:
         return _LIB
-    p = Path(path) if path else lib_path()
+    import os
+
+    p = Path(path or os.environ.get("GALLATIN_GB300_LIB") or lib_path())
     if not p.exists():
         raise GalError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
     lib = ctypes.CDLL(str(p))
@@ -154,7 +166,7 @@ def load(path: str | Path | None = None):
         "gal_reset_counters": (i32, [vp]),
         "gal_dump_bytes": (c_int64, [vp, i32, i32, i32]),
         "gal_dump": (i32, [vp, i32, i32, i32, vp, u64]),
-        "gal_veb_layer_count": (i32, [vp, i32]),
+        "gal_veb_layer_count": (i32, [vp, i32, i32]),
         "gal_malloc_batch": (i32, [vp, vp, u64, vp, vp]),
         "gal_free_batch": (i32, [vp, vp, u64, vp]),
         "gal_flush_pinned": (i32, [vp, vp]),
@@ -353,6 +365,7 @@ class Gallatin:
             "segment_allocations": s.segment_allocations,
             "segments_in_allocations": s.segments_in_allocations,
             "counters": dict(zip(COUNTERS, list(s.counters)[: len(COUNTERS)])),
+            "tree_pins": list(s.counters)[TREE_PIN_COUNTER : TREE_PIN_COUNTER + nt],
         }
 
     def print_info(self) -> None:
@@ -370,12 +383,14 @@ class Gallatin:
         _check(load().gal_dump(self.handle, which, tree, layer, out.ctypes.data, nbytes))
         return out
 
-    def veb_layers(self, tree: int = -1) -> list[np.ndarray]:
-        """All layers (top first) of the segment tree (tree=-1) or sub tree `tree`."""
-        n = load().gal_veb_layer_count(self.handle, tree)
+    def veb_layers(self, tree: int = -1, kind: str = "sub_tree") -> list[np.ndarray]:
+        """All layers (top first) of the segment tree (tree=-1), or of sub tree /
+        adoptable-block tree `tree` (kind "sub_tree" or "adopt_tree")."""
         if tree < 0:
-            return [self.dump("segment_tree", 0, i) for i in range(n)]
-        return [self.dump("sub_tree", tree, i) for i in range(n)]
+            kind = "segment_tree"
+        which = DUMP[kind][0]
+        n = load().gal_veb_layer_count(self.handle, which, max(tree, 0))
+        return [self.dump(kind, max(tree, 0), i) for i in range(n)]
 
 
 class VebTree:

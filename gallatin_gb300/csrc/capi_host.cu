@@ -140,14 +140,20 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   s.ext_blocks_per_segment = s.blocks_per_segment >> (num_trees - 1);
   s.num_sms = (uint32_t)prop.multiProcessorCount;
   s.seed = seed;
-  if (min_slots == 0) min_slots = 8;
+  // Pinned blocks per size class: one per SM for small classes; for large
+  // classes as many as a quarter of the arena split evenly over the classes
+  // affords (a block of class t is 4096 slices of min << t bytes).
+  if (min_slots == 0) min_slots = 4;
+  const uint64_t budget = s.arena_bytes / (4ull * (uint64_t)num_trees);
   uint32_t total = 0;
   for (int t = 0; t < num_trees; ++t) {
-    uint32_t c = (s.num_sms + (1u << t) - 1) >> t;
+    const uint64_t block_bytes = 4096ull * (min_size << t);
+    uint64_t c = budget / block_bytes;
+    if (c > s.num_sms) c = s.num_sms;
     if (c < min_slots) c = min_slots;
-    s.slot_count[t] = c;
+    s.slot_count[t] = (uint32_t)c;
     s.slot_offset[t] = total;
-    total += c;
+    total += (uint32_t)c;
   }
   s.total_slots = total;
 
@@ -202,6 +208,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
     if ((rc = galcapi::build_veb(&s.sub_trees[t], num_segments, seed + (uint64_t)t, false, h->device_allocs)) !=
         GAL_OK)
       return cleanup(rc);
+    if ((rc = galcapi::build_veb(&s.adopt_trees[t], nblocks, seed + (uint64_t)t, false, h->device_allocs)) != GAL_OK)
+      return cleanup(rc);
   }
   if ((rc = device_alloc(h, &h->d_state, 1, "cudaMalloc state")) != GAL_OK) return cleanup(rc);
   if ((rc = try_cuda(cudaMemcpy(h->d_state, &s, sizeof(s), cudaMemcpyHostToDevice), "copy state")))
@@ -255,11 +263,13 @@ extern "C" int gal_geometry(gal_allocator *h, gal_geometry_t *out) {
   return GAL_OK;
 }
 
-extern "C" int gal_veb_layer_count(gal_allocator *h, int tree) {
+extern "C" int gal_veb_layer_count(gal_allocator *h, int which, int tree) {
   if (h == nullptr) return -1;
-  if (tree < 0) return h->hs.segment_tree.num_layers;
-  if (tree >= h->hs.num_trees) return -1;
-  return h->hs.sub_trees[tree].num_layers;
+  if (which == GAL_DUMP_SEGMENT_TREE) return h->hs.segment_tree.num_layers;
+  if (tree < 0 || tree >= h->hs.num_trees) return -1;
+  if (which == GAL_DUMP_SUB_TREE) return h->hs.sub_trees[tree].num_layers;
+  if (which == GAL_DUMP_ADOPT_TREE) return h->hs.adopt_trees[tree].num_layers;
+  return -1;
 }
 
 static bool dump_source(gal_allocator *h, int which, int tree, int layer, const void **src, uint64_t *bytes) {
@@ -276,10 +286,12 @@ static bool dump_source(gal_allocator *h, int which, int tree, int layer, const 
     case GAL_DUMP_COUNTERS: *src = s.counters; *bytes = GAL_NUM_COUNTERS * 8; return true;
     case GAL_DUMP_LOCKS: *src = s.locks; *bytes = 4; return true;
     case GAL_DUMP_SEGMENT_TREE:
-    case GAL_DUMP_SUB_TREE: {
+    case GAL_DUMP_SUB_TREE:
+    case GAL_DUMP_ADOPT_TREE: {
       const gal_veb_t *t = nullptr;
       if (which == GAL_DUMP_SEGMENT_TREE) t = &s.segment_tree;
-      else if (tree >= 0 && tree < s.num_trees) t = &s.sub_trees[tree];
+      else if (tree >= 0 && tree < s.num_trees)
+        t = (which == GAL_DUMP_SUB_TREE) ? &s.sub_trees[tree] : &s.adopt_trees[tree];
       if (t == nullptr || layer < 0 || layer >= t->num_layers) return false;
       *src = t->bits[layer];
       *bytes = t->layer_words[layer] * 8;

@@ -11,13 +11,28 @@
 //   mixed  each thread, for `rounds` rounds: size = 16 << class, where class
 //          is x mod 9 of a per-thread xorshift64 seeded by splitmix64(seed +
 //          tid) or read from a class trace; malloc, fill every 16 bytes with
-//          (tid ^ round), verify, free. Thread 0 of every seg_every-th CTA
+//          (tid ^ round), verify, free. The fill and the verify are done by
+//          the whole warp, one lane's allocation at a time, so each step is a
+//          coalesced 512-byte access. Thread 0 of every seg_every-th CTA
 //          first makes one segment-tier request of a size drawn uniformly in
 //          [seg_lo, seg_hi] and touches its first and last 16 bytes.
+//          Launch with blockDim a multiple of 32 (whole warps).
 #ifndef GALLATIN_GB300_WORKLOADS_CUH
 #define GALLATIN_GB300_WORKLOADS_CUH
 
 #include <stdint.h>
+
+// CTAs per SM the mixed workload kernel is compiled for (0: compiler's
+// choice). The same value applies to every allocator the template is
+// instantiated over.
+#ifndef GALWORK_MIN_BLOCKS
+#define GALWORK_MIN_BLOCKS 4
+#endif
+#if GALWORK_MIN_BLOCKS > 0
+#define GALWORK_MIXED_BOUNDS __launch_bounds__(256, GALWORK_MIN_BLOCKS)
+#else
+#define GALWORK_MIXED_BOUNDS
+#endif
 
 namespace galwork {
 
@@ -45,7 +60,7 @@ __device__ __forceinline__ ulonglong2 load_cg(const ulonglong2 *p) {
 }
 
 template <class Alloc>
-__global__ void pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
+__global__ void __launch_bounds__(1024) pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
   const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
   if (tid >= n) return;
   uint64_t *p = (uint64_t *)alloc->malloc(size);
@@ -59,12 +74,13 @@ __global__ void pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned l
 }
 
 template <class Alloc>
-__global__ void mixed_kernel(Alloc *alloc, uint64_t n, uint32_t rounds, uint64_t seed, uint32_t seg_every,
-                             uint64_t seg_lo, uint64_t seg_hi, const uint8_t *classes,
-                             unsigned long long *stats) {
+__global__ void GALWORK_MIXED_BOUNDS mixed_kernel(Alloc *alloc, uint64_t n, uint32_t rounds, uint64_t seed,
+                                                  uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi,
+                                                  const uint8_t *classes, unsigned long long *stats) {
   const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
-  if (tid >= n) return;
-  if (seg_every != 0 && threadIdx.x == 0 && blockIdx.x % seg_every == 0) {
+  const bool active = tid < n;
+  const uint32_t lane = threadIdx.x & 31;
+  if (active && seg_every != 0 && threadIdx.x == 0 && blockIdx.x % seg_every == 0) {
     const uint64_t j = blockIdx.x / seg_every;
     const uint64_t size = seg_lo + splitmix64(seed + n + j) % (seg_hi - seg_lo + 1);
     ulonglong2 *p = (ulonglong2 *)alloc->malloc(size);
@@ -72,8 +88,8 @@ __global__ void mixed_kernel(Alloc *alloc, uint64_t n, uint32_t rounds, uint64_t
       const uint64_t last = size / 16 - 1;
       p[0] = make_ulonglong2(tid, j);
       p[last] = make_ulonglong2(j, tid);
-      volatile unsigned long long *vp = (volatile unsigned long long *)p;
-      if (vp[0] != tid || vp[2 * last] != j) atomicAdd(stats + STAT_BAD, 1ull);
+      const ulonglong2 a = load_cg(p), b = load_cg(p + last);
+      if (a.x != tid || a.y != j || b.x != j || b.y != tid) atomicAdd(stats + STAT_BAD, 1ull);
       alloc->free(p);
       atomicAdd(stats + STAT_SEG_OK, 1ull);
     } else {
@@ -83,25 +99,37 @@ __global__ void mixed_kernel(Alloc *alloc, uint64_t n, uint32_t rounds, uint64_t
   uint64_t s = splitmix64(seed + tid);
   unsigned long long misses = 0, bad = 0;
   for (uint32_t r = 0; r < rounds; ++r) {
-    const uint32_t cls = classes ? (uint32_t)classes[(uint64_t)r * n + tid] : (uint32_t)(xorshift64(s) % 9);
-    const uint64_t size = 16ull << cls;
-    ulonglong2 *p = (ulonglong2 *)alloc->malloc(size);
-    if (p == nullptr) {
-      ++misses;
-      continue;
-    }
+    ulonglong2 *p = nullptr;
+    uint64_t n16 = 0;
     const uint64_t v = tid ^ r;
-    const ulonglong2 fill = make_ulonglong2(v, v);
-    const uint64_t n16 = size / 16;
-    for (uint64_t i = 0; i < n16; ++i) p[i] = fill;
-    for (uint64_t i = 0; i < n16; ++i) {
-      const ulonglong2 got = load_cg(p + i);
-      if (got.x != v || got.y != v) {
-        ++bad;
-        break;
+    if (active) {
+      const uint32_t cls = classes ? (uint32_t)classes[(uint64_t)r * n + tid] : (uint32_t)(xorshift64(s) % 9);
+      const uint64_t size = 16ull << cls;
+      p = (ulonglong2 *)alloc->malloc(size);
+      if (p == nullptr) {
+        ++misses;
+      } else {
+        n16 = size / 16;
       }
     }
-    alloc->free(p);
+    // The warp fills and verifies each lane's allocation in turn, 32 lanes x
+    // 16 bytes per step: every byte of every allocation is written with its
+    // owner's (tid ^ round) and read back from L2.
+    for (uint32_t j = 0; j < 32; ++j) {
+      ulonglong2 *pj = (ulonglong2 *)__shfl_sync(0xffffffffu, (unsigned long long)p, j);
+      const uint64_t nj = __shfl_sync(0xffffffffu, n16, j);
+      const uint64_t vj = __shfl_sync(0xffffffffu, v, j);
+      if (pj == nullptr) continue;
+      const ulonglong2 fill = make_ulonglong2(vj, vj);
+      for (uint64_t i = lane; i < nj; i += 32) pj[i] = fill;
+      uint64_t diff = 0;
+      for (uint64_t i = lane; i < nj; i += 32) {
+        const ulonglong2 got = load_cg(pj + i);
+        diff |= (got.x ^ vj) | (got.y ^ vj);
+      }
+      if (__any_sync(0xffffffffu, diff != 0) && lane == j) ++bad;
+    }
+    if (p != nullptr) alloc->free(p);
   }
   if (misses) atomicAdd(stats + STAT_MISS, misses);
   if (bad) atomicAdd(stats + STAT_BAD, bad);

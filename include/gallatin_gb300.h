@@ -63,7 +63,9 @@ typedef struct gal_stats_t {
  * min_size and max_size must be powers of two with
  * segment_bytes >= max_size * 4096 (reference static_assert gallatin.cuh:300)
  * and max_size >= 32 * min_size (multi-slice runs fit one bitmap word).
- * min_slots: floor on pinned blocks per size class (0 = default 8).
+ * min_slots: floor on pinned blocks per size class (0 = default 4); the
+ * count per class is otherwise one per SM, capped so a class's pinned blocks
+ * take at most a quarter of the arena divided by the number of classes.
  * Replaces Gallatin<seg,min,max>::generate_on_device. */
 int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size, uint64_t max_size,
                uint32_t min_slots, gal_allocator **out);
@@ -102,9 +104,12 @@ int gal_reset_counters(gal_allocator *h);
 #define GAL_DUMP_SEGMENT_TREE 8
 #define GAL_DUMP_SUB_TREE 9
 #define GAL_DUMP_LOCKS 10
+#define GAL_DUMP_ADOPT_TREE 11
 int64_t gal_dump_bytes(gal_allocator *h, int which, int tree, int layer);
 int gal_dump(gal_allocator *h, int which, int tree, int layer, void *host_dst, uint64_t bytes);
-int gal_veb_layer_count(gal_allocator *h, int tree); /* tree -1 = segment tree */
+/* layers of a vEB tree of this allocator: which is GAL_DUMP_SEGMENT_TREE,
+ * GAL_DUMP_SUB_TREE or GAL_DUMP_ADOPT_TREE (tree selects the size class) */
+int gal_veb_layer_count(gal_allocator *h, int which, int tree);
 
 /* --- batch entry points (device buffers, one thread per request) ---
  * These are the host-callable form of Gallatin::malloc / free

@@ -37,6 +37,9 @@ constexpr int kClaimSteps = 160;          // fetch-and steps per reservation
 constexpr int kRequestBlockAttempts = 512;
 constexpr int kSegmentLockSpins = 1 << 20;
 constexpr int kSegmentLockBit = 31;
+// a pinned block past this many live slices is replaced ahead of time, so
+// warps rarely find their slot's block full
+constexpr uint32_t kRefillMark = GAL_BLOCK_SLICES * 7 / 8;
 
 enum { TIER_SLICE = 0, TIER_BLOCK = 1, TIER_SEGMENT = 2 };
 
@@ -163,16 +166,34 @@ __device__ __forceinline__ void unlock(const gal_state_t *st, int bit) {
 
 // ---- segments ------------------------------------------------------------
 
-__device__ inline void sub_tree_cleanup(const gal_state_t *st, uint32_t t, uint64_t seg) {
-  veb::remove(&st->sub_trees[t], seg);
-  if (ptx::ld_relaxed(st->chunk_ids + seg) == t && ptx::ld_relaxed(st->seg_avail + seg) > 0) {
-    veb::insert_force_update(&st->sub_trees[t], seg);
+// A segment belongs in sub tree t exactly while it is formatted for t and has
+// a free block. Callers that change either fact call this afterwards: it
+// applies the membership it observes and re-reads until the observation is
+// stable, so the last change always wins. Under contention a segment can be
+// listed without a free block for a moment (searches then fail on it and
+// sync it again); it is never left unlisted while it has a free block.
+__device__ __forceinline__ bool seg_listed_for(const gal_state_t *st, uint32_t t, uint64_t seg) {
+  return ptx::ld_relaxed(st->chunk_ids + seg) == t && ptx::ld_relaxed(st->seg_avail + seg) > 0;
+}
+
+__device__ inline void sub_tree_sync(const gal_state_t *st, uint32_t t, uint64_t seg) {
+  const gal_veb_t *sub = &st->sub_trees[t];
+  bool want = seg_listed_for(st, t, seg);
+  for (int i = 0; i < 8; ++i) {
+    if (want) {
+      veb::insert_force_update(sub, seg);
+    } else {
+      veb::remove(sub, seg);
+    }
+    const bool now = seg_listed_for(st, t, seg);
+    if (now == want) return;
+    want = now;
   }
 }
 
 __device__ inline void try_retire_segment(const gal_state_t *st, uint64_t seg, uint32_t t, int32_t bps_t) {
   if (ptx::cas_acq_rel(st->seg_avail + seg, bps_t, (int32_t)GAL_SEG_GATE) != bps_t) return;
-  veb::remove(&st->sub_trees[t], seg);
+  sub_tree_sync(st, t, seg);
   unsigned short prev = atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)t,
                                   (unsigned short)GAL_FREE_SEGMENT);
   if (prev != (unsigned short)t) count(st, GAL_CTR_CORRUPT);
@@ -192,7 +213,7 @@ __device__ inline void seg_avail_add_one(const gal_state_t *st, uint64_t seg) {
   if (now == bps_t) {
     try_retire_segment(st, seg, t, bps_t);
   } else if (now == 1) {
-    veb::insert_force_update(&st->sub_trees[t], seg);
+    sub_tree_sync(st, t, seg);
   }
 }
 
@@ -216,7 +237,7 @@ __device__ inline uint64_t attach_segment(const gal_state_t *st, uint32_t t) {
     ptx::st_relaxed(words + w, v);
   }
   ptx::atom_add_release(st->seg_avail + seg, (int32_t)bps_t - (int32_t)GAL_SEG_GATE);
-  veb::insert_force_update(&st->sub_trees[t], seg);
+  sub_tree_sync(st, t, seg);
   count(st, GAL_CTR_SEGMENT_ATTACH);
   return seg;
 }
@@ -227,15 +248,15 @@ __device__ inline uint32_t take_block(const gal_state_t *st, uint64_t seg, uint3
   const int32_t before = ptx::atom_add_acquire(st->seg_avail + seg, -1);
   if (before <= 0) {
     seg_avail_add_one(st, seg);
-    sub_tree_cleanup(st, t, seg);
+    sub_tree_sync(st, t, seg);
     return GAL_EMPTY_BLOCK;
   }
   if (ptx::ld_relaxed(st->chunk_ids + seg) != t) {
     seg_avail_add_one(st, seg);
-    sub_tree_cleanup(st, t, seg);
+    sub_tree_sync(st, t, seg);
     return GAL_EMPTY_BLOCK;
   }
-  if (before == 1) sub_tree_cleanup(st, t, seg);
+  if (before == 1) sub_tree_sync(st, t, seg);
   uint64_t *words = st->seg_block_bits + seg * st->seg_block_words;
   const int bis = block_index_shift(st);
   for (int pass = 0; pass < 64; ++pass) {
@@ -264,6 +285,27 @@ __device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b
   count(st, GAL_CTR_BLOCK_RETIRE);
 }
 
+// A block belongs in adoptable tree t exactly while it is DETACHED and
+// formatted for t (same apply-then-confirm discipline as sub_tree_sync).
+__device__ inline void adopt_sync(const gal_state_t *st, uint32_t t, uint64_t b) {
+  const gal_veb_t *at = &st->adopt_trees[t];
+  auto listed = [&]() {
+    const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
+    return meta_state(m) == GAL_STATE_DETACHED && meta_tree(m) == t;
+  };
+  bool want = listed();
+  for (int i = 0; i < 8; ++i) {
+    if (want) {
+      veb::insert_force_update(at, b);
+    } else {
+      veb::remove(at, b);
+    }
+    const bool now = listed();
+    if (now == want) return;
+    want = now;
+  }
+}
+
 // A DETACHED block whose live count reached zero goes back to its segment.
 __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
   uint64_t *mp = st->block_meta + b;
@@ -273,6 +315,7 @@ __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
     const uint64_t nm = m - ((uint64_t)GAL_STATE_DETACHED << GAL_META_STATE_SHIFT);
     const uint64_t r = ptx::cas_acq_rel(mp, m, nm);
     if (r == m) {
+      adopt_sync(st, meta_tree(m), b);
       return_block_to_segment(st, b);
       return;
     }
@@ -301,9 +344,37 @@ __device__ __forceinline__ uint64_t mix_tid(uint64_t tid, int attempt) {
   return attempt == 0 ? tid : murmur64a_u64(tid, (uint64_t)attempt);
 }
 
+// Pin again a DETACHED block of tree t that still has room (used only when no
+// fresh block can be had). The block keeps its live slices and bitmap.
+__device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t t) {
+  const gal_veb_t *at = &st->adopt_trees[t];
+  uint64_t cand = veb::find_first_valid_index(at);
+  for (int k = 0; k < 64 && cand != veb::kFail; ++k) {
+    uint64_t m = ptx::ld_relaxed(st->block_meta + cand);
+    for (int i = 0; i < 8; ++i) {
+      if (meta_state(m) != GAL_STATE_DETACHED || meta_tree(m) != t || meta_live(m) >= GAL_BLOCK_SLICES) break;
+      const uint64_t nm = m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
+      const uint64_t r = ptx::cas_acq_rel(st->block_meta + cand, m, nm);
+      if (r == m) {
+        adopt_sync(st, t, cand);
+        count(st, GAL_CTR_ADOPT);
+        return (uint32_t)cand;
+      }
+      m = r;
+    }
+    if (meta_state(m) != GAL_STATE_DETACHED || meta_tree(m) != t) adopt_sync(st, t, cand);
+    cand = veb::successor_thorough(at, cand);
+  }
+  return GAL_EMPTY_BLOCK;
+}
+
 // A FREE block of tree t, from a segment already formatted for t or from a
-// newly attached one. GAL_EMPTY_BLOCK when the arena cannot provide one.
-__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint64_t tid) {
+// newly attached one. When the arena has neither and allow_adopt is set, a
+// DETACHED block with room is pinned again instead (*adopted = true; it is
+// already PINNED). GAL_EMPTY_BLOCK when nothing can be had.
+__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint64_t tid, bool allow_adopt,
+                                         bool *adopted) {
+  *adopted = false;
   const gal_veb_t *sub = &st->sub_trees[t];
   for (int a = 0; a < kRequestBlockAttempts; ++a) {
     uint64_t seg = veb::find_random_valid_index(sub, mix_tid(tid, a));
@@ -312,8 +383,11 @@ __device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint
         seg = attach_segment(st, t);
         unlock(st, (int)t);
         if (seg == veb::kFail) {
-          if (veb::find_first_valid_index(sub) == veb::kFail) return GAL_EMPTY_BLOCK;
-          continue;
+          if (veb::find_first_valid_index(sub) != veb::kFail) continue;
+          if (!allow_adopt) return GAL_EMPTY_BLOCK;
+          const uint32_t b = adopt_block(st, t);
+          *adopted = b != GAL_EMPTY_BLOCK;
+          return b;
         }
       } else {
         backoff(a);
@@ -340,25 +414,31 @@ __device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t) 
   }
   own_block(st, b, t, GAL_STATE_PINNED, 0);  // release: bitmap before PINNED
   count(st, GAL_CTR_BLOCK_PINS);
+  count(st, GAL_CTR_TREE_PINS + (int)t);
 }
 
 __device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) {
   const uint64_t old = ptx::atom_add_release(
       st->block_meta + b, (uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
-  if (meta_live(old) == 0) try_retire_block(st, b);
+  if (meta_live(old) == 0) {
+    try_retire_block(st, b);
+  } else {
+    adopt_sync(st, meta_tree(old), b);
+  }
 }
 
 // Replace the block a slot holds (`seen`, without the REPLACING flag) by a
 // freshly pinned one. Only the thread whose CAS sets REPLACING does the work.
 __device__ inline uint32_t replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t,
-                                        uint64_t tid) {
+                                        uint64_t tid, bool allow_adopt = true) {
   if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return GAL_EMPTY_BLOCK;
-  const uint32_t nb = request_block(st, t, tid);
+  bool adopted = false;
+  const uint32_t nb = request_block(st, t, tid, allow_adopt, &adopted);
   if (nb == GAL_EMPTY_BLOCK) {
     ptx::st_release(slot, seen);
     return GAL_EMPTY_BLOCK;
   }
-  pin_block(st, nb, t);
+  if (!adopted) pin_block(st, nb, t);
   ptx::st_release(slot, (uint64_t)nb);
   if ((uint32_t)seen != GAL_EMPTY_BLOCK) detach_block(st, (uint32_t)seen);
   return nb;
@@ -394,42 +474,58 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
     uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
+    bool refill = false;
     if (lane == (uint32_t)leader) {
       const uint64_t sv = ptx::ld_acquire(slot);
-      if (sv & GAL_SLOT_REPLACING) {
-        backoff(attempt);
-      } else {
-        b = (uint32_t)sv;
-        if (b == GAL_EMPTY_BLOCK) b = replace_slot(st, slot, sv, t, tid);
-        if (b != GAL_EMPTY_BLOCK) {
-          uint64_t m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)need << GAL_META_CURSOR_SHIFT) | need);
-          take = g_n;
-          if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED) {
-            release_live(st, b, need);
-            take = 0;
-          } else if (meta_live(m) + need > GAL_BLOCK_SLICES) {
-            // full for the whole group: undo, then reserve what still fits
-            release_live(st, b, need);
-            const uint32_t room = meta_live(m) < GAL_BLOCK_SLICES ? GAL_BLOCK_SLICES - meta_live(m) : 0;
-            take = room / c < g_n ? room / c : g_n;
-            if (take > 0) {
-              const uint32_t part = take * c;
-              m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)part << GAL_META_CURSOR_SHIFT) | part);
-              if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED ||
-                  meta_live(m) + part > GAL_BLOCK_SLICES) {
-                release_live(st, b, part);
-                take = 0;
-              }
-            }
-            if (take == 0) replace_slot(st, slot, (uint64_t)b, t, tid);
-          }
-          if (take > 0) {
-            cursor = meta_cursor(m) & (GAL_BLOCK_SLICES - 1);
-          } else {
-            b = GAL_EMPTY_BLOCK;
-          }
+      const bool replacing = (sv & GAL_SLOT_REPLACING) != 0;
+      b = (uint32_t)sv;
+      if (b == GAL_EMPTY_BLOCK) {
+        if (!replacing) {
+          count(st, GAL_CTR_REPLACE_EMPTY);
+          b = replace_slot(st, slot, sv, t, tid);
         } else {
+          count(st, GAL_CTR_SLOT_BUSY);
           backoff(attempt);
+        }
+      }
+      if (b != GAL_EMPTY_BLOCK) {
+        // the block stays usable while another leader replaces it
+        uint64_t m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)need << GAL_META_CURSOR_SHIFT) | need);
+        take = g_n;
+        if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED) {
+          release_live(st, b, need);
+          count(st, GAL_CTR_STALE_SLOT);
+          take = 0;
+        } else if (meta_live(m) + need > GAL_BLOCK_SLICES) {
+          // full for the whole group: undo, then reserve what still fits
+          release_live(st, b, need);
+          const uint32_t room = meta_live(m) < GAL_BLOCK_SLICES ? GAL_BLOCK_SLICES - meta_live(m) : 0;
+          take = room / c < g_n ? room / c : g_n;
+          if (take > 0) {
+            const uint32_t part = take * c;
+            m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)part << GAL_META_CURSOR_SHIFT) | part);
+            if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED ||
+                meta_live(m) + part > GAL_BLOCK_SLICES) {
+              release_live(st, b, part);
+              take = 0;
+            }
+          }
+          if (take == 0) {
+            if (!replacing) {
+              count(st, GAL_CTR_REPLACE_FULL);
+              replace_slot(st, slot, (uint64_t)b, t, tid);
+            } else {
+              count(st, GAL_CTR_SLOT_BUSY);
+              backoff(attempt);
+            }
+          }
+        } else if (!replacing && meta_live(m) + need > kRefillMark) {
+          refill = true;  // swap in a fresh block once this group is served
+        }
+        if (take > 0) {
+          cursor = meta_cursor(m) & (GAL_BLOCK_SLICES - 1);
+        } else {
+          b = GAL_EMPTY_BLOCK;
         }
       }
     }
@@ -474,13 +570,21 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
     }
     if (acc < take && lane == (uint32_t)leader) {
       release_live(st, b, (take - acc) * c);
+      count(st, GAL_CTR_CLAIM_SHORT);
       // a reservation that found no aligned run: the block is too fragmented
       // for this run length, so give the slot a fresh block
-      if (c > 1) replace_slot(st, slot, (uint64_t)b, t, tid);
+      if (c > 1) {
+        count(st, GAL_CTR_REPLACE_FRAG);
+        replace_slot(st, slot, (uint64_t)b, t, tid);
+      }
     }
     if (my_slice >= 0) {
       result = block_address(st, b, t) + ((uint64_t)my_slice << (st->min_shift + (int)t));
       done = true;
+    }
+    if (refill && lane == (uint32_t)leader) {
+      count(st, GAL_CTR_REPLACE_REFILL);
+      replace_slot(st, slot, (uint64_t)b, t, tid, false);  // fresh blocks only
     }
   }
   if (!done) count(st, GAL_CTR_OOM_SLICE);
@@ -526,7 +630,8 @@ __device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t 
 // ---- block and segment tiers ---------------------------------------------
 
 __device__ inline void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_t tid) {
-  const uint32_t b = request_block(st, bt, tid);
+  bool adopted = false;
+  const uint32_t b = request_block(st, bt, tid, false, &adopted);
   if (b == GAL_EMPTY_BLOCK) {
     count(st, GAL_CTR_OOM_BLOCK);
     return nullptr;

@@ -19,7 +19,9 @@
  *   block_ext       u64[num_segments * ext_blocks_per_segment * 64] marks the
  *                   continuation slices of multi-slice runs (largest tree only)
  *   slots           u64[total_slots]    pinned block per (tree, SM slot)
- *   veb bit layers  one u64 array per layer per tree
+ *   veb bit layers  one u64 array per layer per tree: the segment tree and
+ *                   the per-tree sub trees over segment ids, and the per-tree
+ *                   adoptable-block trees over block ids
  */
 #ifndef GALLATIN_GB300_STATE_H
 #define GALLATIN_GB300_STATE_H
@@ -68,7 +70,16 @@ enum gal_counter_id {
   GAL_CTR_SEGMENT_ATTACH = 7,
   GAL_CTR_SEGMENT_RETIRE = 8,
   GAL_CTR_BLOCK_RETIRE = 9,
-  GAL_NUM_COUNTERS = 16
+  GAL_CTR_REPLACE_EMPTY = 10, /* slot had no block yet */
+  GAL_CTR_REPLACE_FULL = 11,  /* pinned block had no room left */
+  GAL_CTR_REPLACE_FRAG = 12,  /* no aligned run for a multi-slice request */
+  GAL_CTR_CLAIM_SHORT = 13,   /* reservation held but bits not found in time */
+  GAL_CTR_STALE_SLOT = 14,    /* slot changed between read and reservation */
+  GAL_CTR_SLOT_BUSY = 15,     /* slot was being replaced */
+  GAL_CTR_REPLACE_REFILL = 16, /* pinned block replaced ahead of filling up */
+  GAL_CTR_ADOPT = 17,          /* detached block with room pinned again */
+  GAL_CTR_TREE_PINS = 32,     /* + tree id: blocks pinned per tree */
+  GAL_NUM_COUNTERS = 64
 };
 
 typedef struct gal_veb_t {
@@ -113,6 +124,9 @@ typedef struct gal_state_t {
 
   gal_veb_t segment_tree;
   gal_veb_t sub_trees[GAL_MAX_TREES];
+  /* per tree: DETACHED blocks (universe = all block ids) that a slot can pin
+   * again when no fresh block is left, so their free slices stay reachable */
+  gal_veb_t adopt_trees[GAL_MAX_TREES];
 } gal_state_t;
 
 #endif /* GALLATIN_GB300_STATE_H */

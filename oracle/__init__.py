@@ -118,6 +118,12 @@ def load_ref(build_if_missing: bool = True):
     global _REF
     if _REF is not None:
         return _REF
+    import os
+
+    override = os.environ.get("GALLATIN_REF_LIB")
+    if override:
+        _REF = _bind_ref(ctypes.CDLL(override))
+        return _REF
     if build_if_missing and not build.ref_lib().exists():
         try:
             build.build_reference()
@@ -125,7 +131,11 @@ def load_ref(build_if_missing: bool = True):
             return None
     if not build.ref_lib().exists():
         return None
-    lib = ctypes.CDLL(str(build.ref_lib()))
+    _REF = _bind_ref(ctypes.CDLL(str(build.ref_lib())))
+    return _REF
+
+
+def _bind_ref(lib):
     vp, u64, u32, i32 = c_void_p, c_uint64, c_uint32, c_int
     sigs = {
         "galref_veb_create": (i32, [u64, u64, POINTER(vp)]),
@@ -144,7 +154,6 @@ def load_ref(build_if_missing: bool = True):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _REF = lib
     return lib
 
 

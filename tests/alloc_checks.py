@@ -85,6 +85,8 @@ def check_restored(alloc: gal.Gallatin) -> None:
     for t in range(alloc.num_trees):
         for layer in alloc.veb_layers(t):
             assert not layer.any(), f"sub tree {t} not empty"
+        for layer in alloc.veb_layers(t, "adopt_tree"):
+            assert not layer.any(), f"adoptable-block tree {t} not empty"
     ids = alloc.dump("chunk_ids")
     assert (ids == gal.GAL_FREE_SEGMENT).all(), "memory table not reset"
     avail = alloc.dump("seg_avail")

@@ -34,16 +34,42 @@ def release_all(torch, alloc, ptrs) -> None:
 
 TIER_SIZES = [1, 16, 17, 33, 100, 256, 1000, 2048, 4096, 4097, 8192, 12000, 32768, 40000, 1 << 20, 3 << 20,
               16 << 20, (16 << 20) + 1, 50 << 20]
+TIER_P = np.array([8, 8, 8, 8, 8, 8, 8, 8, 8, 4, 4, 4, 4, 2, 1, 1, 0.5, 0.3, 0.2])
+
+
+def longest_free_run(alloc) -> int:
+    leaf = alloc.veb_layers(-1)[-1]
+    bits = np.unpackbits(leaf.view(np.uint8), bitorder="little")[: alloc.num_segments]
+    longest = run = 0
+    for b in bits:
+        run = run + 1 if b else 0
+        longest = max(longest, run)
+    return longest
+
+
+def check_nulls_justified(alloc, ptrs, sizes) -> None:
+    """In a malloc-only phase the free space only shrinks, so every null must
+    still be justified by the end state: no free run long enough for a
+    segment-tier request, and no free segment at all for the other tiers."""
+    failed = sizes[ptrs == 0]
+    if failed.size == 0:
+        return
+    longest = longest_free_run(alloc)
+    for s in failed:
+        tier, _, cnt = gal.classify(int(s), alloc.min_size, alloc.max_size, alloc.segment_size)
+        need = cnt if tier == "segment" else 1
+        assert longest < need, f"request of {int(s)} B failed while {longest} contiguous segments are free"
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_mixed_tiers_batch(cuda, seed):
     rng = np.random.default_rng(seed)
     with gal.Gallatin.generate_on_device(2 << 30, seed, print_info=False) as a:
-        sizes = rng.choice(TIER_SIZES, size=20000, p=None).astype(np.uint64)
+        sizes = rng.choice(TIER_SIZES, size=20000, p=TIER_P / TIER_P.sum()).astype(np.uint64)
         ptrs = malloc_batch(cuda, a, sizes)
-        spans = check_live(a, ptrs, sizes)
-        assert len(spans) > 0.5 * len(sizes)
+        check_live(a, ptrs, sizes)
+        check_nulls_justified(a, ptrs, sizes)
+        assert (ptrs != 0).mean() > 0.5
         release_all(cuda, a, ptrs)
 
 
@@ -70,8 +96,9 @@ def test_one_class_packs_blocks(cuda):
         assert (ptrs != 0).all()
         check_live(a, ptrs, np.full(n, 16, dtype=np.uint64))
         blocks = np.unique((ptrs - np.uint64(a.arena_base)) >> np.uint64(16))
-        # 4096 slices per 64 KiB block; partly filled pinned blocks allowed
-        assert len(blocks) <= n // 4096 + a.slot_count[0]
+        # 4096 slices per 64 KiB block; a pinned block is swapped out once it
+        # holds 7/8 of that, and partly filled pinned blocks remain
+        assert len(blocks) <= n // (4096 * 7 // 8) + a.slot_count[0]
         release_all(cuda, a, ptrs)
 
 
@@ -105,15 +132,8 @@ def test_segment_tier_fails_only_without_a_free_run(cuda):
         sizes = (rng.integers(1, 9, size=40) * (16 << 20)).astype(np.uint64)
         ptrs = malloc_batch(cuda, a, sizes)
         check_live(a, ptrs, sizes)
-        leaf = a.veb_layers(-1)[-1]
-        bits = np.unpackbits(leaf.view(np.uint8), bitorder="little")[: a.num_segments]
-        longest, run = 0, 0
-        for b in bits:
-            run = run + 1 if b else 0
-            longest = max(longest, run)
-        for p, s in zip(ptrs, sizes):
-            if p == 0:
-                assert longest < int(s) // (16 << 20), "segment request failed while a long enough run is free"
+        check_nulls_justified(a, ptrs, sizes)
+        assert (ptrs != 0).any()
         release_all(cuda, a, ptrs)
 
 
