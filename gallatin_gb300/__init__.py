@@ -45,6 +45,7 @@ GAL_NUM_COUNTERS = 64
 GAL_EMPTY_BLOCK = 0xFFFFFFFF
 GAL_FREE_SEGMENT = 0xFFFF
 GAL_SEG_GATE = -(1 << 28)
+NOALLOC_TRACE_MAX_BYTES = 2 << 20
 
 OPS = {
     "insert": 0,
@@ -173,6 +174,7 @@ def load(path: str | Path | None = None):
         "gal_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "gal_run_mixed_host_noalloc": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
         "gal_veb_destroy": (i32, [vp]),
         "gal_veb_num_layers": (i32, [vp]),
@@ -336,6 +338,41 @@ class Gallatin:
         out = np.zeros(8, dtype=np.uint64)
         _check(
             load().gal_run_mixed_host(
+                self.handle,
+                n_threads,
+                rounds,
+                seed,
+                seg_every,
+                seg_lo,
+                seg_hi,
+                h_classes_ptr,
+                block_dim,
+                out.ctypes.data,
+                stream,
+            )
+        )
+        return out
+
+    def run_mixed_host_noalloc(
+        self,
+        n_threads: int,
+        rounds: int,
+        seed: int,
+        h_classes_ptr: int,
+        *,
+        seg_every: int = 0,
+        seg_lo: int = 16 << 20,
+        seg_hi: int = 256 << 20,
+        block_dim: int = 256,
+        stream: int = 0,
+    ) -> np.ndarray:
+        """run_mixed_host for callers that may not allocate device memory.
+
+        The scratch is a fixed array inside the library (at most
+        NOALLOC_TRACE_MAX_BYTES of trace); concurrent calls share it and race."""
+        out = np.zeros(8, dtype=np.uint64)
+        _check(
+            load().gal_run_mixed_host_noalloc(
                 self.handle,
                 n_threads,
                 rounds,

@@ -141,6 +141,25 @@ int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, ui
                        uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes, uint32_t block_dim,
                        uint64_t *h_stats, void *stream);
 
+/* Same as gal_run_mixed_host, but the call allocates no device memory: no
+ * cudaMalloc, no cudaFree, no allocating library routine. It is for callers
+ * that may not allocate at run time, such as a serving loop that cannot take
+ * the device-wide synchronisation a cudaMalloc implies, or a process whose
+ * device memory was divided up in advance. Its scratch (the trace copy and
+ * the stats words) is a fixed array of GAL_NOALLOC_TRACE_MAX_BYTES + 256
+ * bytes compiled into the library, which every GPU that loads the library
+ * holds until the process exits; traces larger than
+ * GAL_NOALLOC_TRACE_MAX_BYTES (n_threads * rounds) are rejected with
+ * GAL_ERR_INVALID. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the one array: calls whose GPU work overlaps
+ * (other streams, other host threads) race on it. No counterpart in the
+ * reference, which allocates its buffers with cudaMalloc. */
+#define GAL_NOALLOC_TRACE_MAX_BYTES (2ull << 20)
+int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
+                               uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,
+                               uint32_t block_dim, uint64_t *h_stats, void *stream);
+
 /* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
 
 typedef struct gal_veb_op {
