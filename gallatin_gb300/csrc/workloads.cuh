@@ -114,7 +114,10 @@ __global__ void GALWORK_MIXED_BOUNDS mixed_kernel(Alloc *alloc, uint64_t n, uint
     }
     // The warp fills and verifies each lane's allocation in turn, 32 lanes x
     // 16 bytes per step: every byte of every allocation is written with its
-    // owner's (tid ^ round) and read back from L2.
+    // owner's (tid ^ round) and read back from L2. Mismatches are collected
+    // per buffer in a mask and reduced once, so the loads of all 32 buffers
+    // can be in flight together.
+    uint32_t mismatch = 0;
     for (uint32_t j = 0; j < 32; ++j) {
       ulonglong2 *pj = (ulonglong2 *)__shfl_sync(0xffffffffu, (unsigned long long)p, j);
       const uint64_t nj = __shfl_sync(0xffffffffu, n16, j);
@@ -127,8 +130,9 @@ __global__ void GALWORK_MIXED_BOUNDS mixed_kernel(Alloc *alloc, uint64_t n, uint
         const ulonglong2 got = load_cg(pj + i);
         diff |= (got.x ^ vj) | (got.y ^ vj);
       }
-      if (__any_sync(0xffffffffu, diff != 0) && lane == j) ++bad;
+      mismatch |= (uint32_t)(diff != 0) << j;
     }
+    if ((__reduce_or_sync(0xffffffffu, mismatch) >> lane) & 1u) ++bad;
     if (p != nullptr) alloc->free(p);
   }
   if (misses) atomicAdd(stats + STAT_MISS, misses);
