@@ -45,6 +45,9 @@ WORKLOADS = {
         seg_every=64, seg_lo=16 * MIB, seg_hi=256 * MIB,
     ),
     "pairs": dict(arena=2 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=1_048_576, size=16, block=1024),
+    # the batching configuration: 64 batches of 1k-512k requests, lognormal
+    # sizes, 60/40 malloc/free over the live set, plus a drain batch
+    "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32),
     # the mixed workload without its 256 segment-tier requests: only the
     # slice tier runs, which is what the reference arm can be compared on
     "mixed-slices": dict(
@@ -179,6 +182,14 @@ def cpu_baseline(name: str, w: dict) -> dict:
         )
         units = n * rounds + (n // w["block"] // w["seg_every"] if w["seg_every"] else 0)
         sample = f"full workload: {n} threads x {rounds} rounds + segment-tier requests, glibc malloc/free"
+    elif name == "batches":
+        from gallatin_gb300.workload import batch_trace
+
+        reqs, offsets, slots, _ = batch_trace(42, n_batches=w["batches"])
+        secs, misses = oracle.cpu_replay_batches(reqs, offsets, slots, cores)
+        bad = 0
+        units = int(offsets[-1])
+        sample = f"full request stream: {units} requests in {len(offsets) - 1} batches, glibc malloc/free"
     else:
         n = w["threads"]
         secs, misses, bad = oracle.cpu_replay_pairs(n, w["size"], cores)
@@ -186,7 +197,7 @@ def cpu_baseline(name: str, w: dict) -> dict:
         sample = f"full workload: {n} threads, glibc malloc/free of {w['size']} B"
     return {
         "value": units / secs,
-        "unit": "malloc+free pairs/s",
+        "unit": "requests/s" if name == "batches" else "malloc+free pairs/s",
         "cores": cores,
         "kind": "port",
         "sample": sample + " (the reference has no CPU implementation; this replays the trace through glibc)",
@@ -242,6 +253,7 @@ def run(args) -> dict | None:
 
         gal.load()
 
+    unit = "requests/s" if args.workload == "batches" else "malloc+free pairs/s"
     stream = torch.cuda.current_stream()
     s_ptr = stream.cuda_stream
     a = make_allocator(impl, w)
@@ -273,6 +285,43 @@ def run(args) -> dict | None:
             "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
             "max_size": w["max_size"], "threads": n, "rounds": rounds, "block_dim": w["block"],
             "segment_tier_requests": seg_requests, "segment_tier_bytes": [w["seg_lo"], w["seg_hi"]], "seed": 42,
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
+    elif args.workload == "batches":
+        from gallatin_gb300.workload import batch_trace
+
+        reqs, offsets, slots, info = batch_trace(42, n_batches=w["batches"])
+        units = int(offsets[-1])
+        alg_bytes = units * 8  # the live-set table entry each request writes
+        d_reqs = torch.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = torch.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = torch.zeros(slots + 1, dtype=torch.int64, device="cuda")
+        h_reqs = torch.from_numpy(reqs.view(np.int64)).pin_memory()
+        bargs = (d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(), stats.data_ptr())
+        if impl == "reference":
+            def step():
+                a.run_batches(*bargs, persistent=False, stream=s_ptr)
+
+            e2e_step = None
+        else:
+            graph = a.capture_batches(*bargs, width=w["width"], persistent=True)
+
+            def step():
+                graph.launch(s_ptr)
+
+            def e2e_step():
+                return a.run_batches_host(reqs, offsets, slots, width=w["width"], persistent=True, stream=s_ptr,
+                                          reqs_ptr=h_reqs.data_ptr())
+
+        h2d = units * 8 + len(offsets) * 8
+        config = {
+            "workload": "batching: 64 batches of U[1k,512k] requests, lognormal(ln 256, 1.5) sizes in [16 B, 64 MiB], "
+                        "60/40 malloc/free over the live set, then a drain batch",
+            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+            "max_size": w["max_size"], "requests": units, "mallocs": info["mallocs"], "frees": info["frees"],
+            "max_live": info["max_live"], "max_request_bytes": info["max_request_bytes"], "seed": 42,
+            "path": ("reference: one launch per batch" if impl == "reference"
+                     else f"persistent cooperative kernel in a CUDA graph, aggregation width {w['width']}"),
             "l2": "flushed (256 MiB write) before every timed step",
         }
     else:
@@ -333,7 +382,7 @@ def run(args) -> dict | None:
         e2e_total = barrier_max(torch, world, float(sum(e2e_times)))
         e2e = {
             "value": units * args.steps * world / e2e_total,
-            "unit": "malloc+free pairs/s",
+            "unit": unit,
             "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": 64,
             "ms_per_step": 1e3 * e2e_total / args.steps,
@@ -362,9 +411,10 @@ def run(args) -> dict | None:
             pass
 
     result = {
-        "metric": "malloc+free ops/s (one op = one malloc + its free)",
+        "metric": ("malloc+free ops/s (one op = one malloc or one free request)" if args.workload == "batches"
+                   else "malloc+free ops/s (one op = one malloc + its free)"),
         "value": value,
-        "unit": "malloc+free pairs/s",
+        "unit": unit,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -385,16 +435,27 @@ def run(args) -> dict | None:
         "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
         "step_ms": times,
     }
-    if impl == "gb300":
+    if args.workload == "batches" and impl == "gb300":
+        graph.close()
+        if args.autotune:
+            from gallatin_gb300.autotune import autotune_batches
+
+            close_allocator(impl, a)
+            a = None
+            result_autotune = autotune_batches(reqs, offsets, slots, arena=w["arena"])
+    if impl == "gb300" and a is not None:
         st_all = a.stats()
         result["allocator_counters"] = st_all["counters"]
         result["tree_pins"] = st_all["tree_pins"]
-    close_allocator(impl, a)
+    if a is not None:
+        close_allocator(impl, a)
+    if args.workload == "batches" and impl == "gb300" and args.autotune:
+        result["autotune"] = result_autotune
     if rank == 0 and impl == "gb300" and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, w)
     if impl == "reference":
         result["cpu_baseline"] = {
-            "value": value, "unit": "malloc+free pairs/s", "cores": 0, "kind": "reference",
+            "value": value, "unit": unit, "cores": 0, "kind": "reference",
             "sample": "the reference's own CUDA build on this GPU (it has no CPU path), full workload",
         }
     if world > 1:
@@ -416,6 +477,7 @@ def main() -> int:
     ap.add_argument("--threads", type=int, default=0, help="override the thread count (small profiling cases)")
     ap.add_argument("--rounds", type=int, default=0, help="override the rounds of the mixed workload")
     ap.add_argument("--arena-gib", type=float, default=0.0, help="override the arena size")
+    ap.add_argument("--autotune", action="store_true", help="batches workload: add the segment x width sweep")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     res = run(args)

@@ -70,13 +70,13 @@ DUMP = {
     "seg_block_bits": (2, np.uint64),
     "block_meta": (3, np.uint64),
     "block_bits": (4, np.uint64),
-    "block_ext": (5, np.uint64),
     "slots": (6, np.uint64),
     "counters": (7, np.uint64),
     "segment_tree": (8, np.uint64),
     "sub_tree": (9, np.uint64),
     "locks": (10, np.uint32),
     "adopt_tree": (11, np.uint64),
+    "roomy_tree": (12, np.uint64),
 }
 
 COUNTERS = [
@@ -98,6 +98,8 @@ COUNTERS = [
     "slot_busy",
     "replace_refill",
     "adopt",
+    "adopt_roomy",
+    "nomem",
 ]
 TREE_PIN_COUNTER = 32
 
@@ -118,6 +120,8 @@ class _Geometry(ctypes.Structure):
         ("num_sms", c_uint32),
         ("total_slots", c_uint32),
         ("slot_count", c_uint32 * GAL_MAX_TREES),
+        ("num_classes", c_uint32),
+        ("pad_", c_uint32),
         ("arena_base", c_uint64),
     ]
 
@@ -175,6 +179,11 @@ def load(path: str | Path | None = None):
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host_noalloc": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "gal_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, vp, vp]),
+        "gal_capture_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, vp, POINTER(vp)]),
+        "gal_graph_launch": (i32, [vp, vp]),
+        "gal_graph_destroy": (i32, [vp]),
+        "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, vp, vp]),
         "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
         "gal_veb_destroy": (i32, [vp]),
         "gal_veb_num_layers": (i32, [vp]),
@@ -240,7 +249,8 @@ class Gallatin:
         self.blocks_per_segment = g.blocks_per_segment
         self.num_sms = g.num_sms
         self.total_slots = g.total_slots
-        self.slot_count = list(g.slot_count)[: g.num_trees]
+        self.num_classes = g.num_classes
+        self.slot_count = list(g.slot_count)[: g.num_classes]
         self.arena_base = g.arena_base
 
     @classmethod
@@ -388,6 +398,33 @@ class Gallatin:
         )
         return out
 
+    # -- batched request streams ---------------------------------------------
+    def run_batches(self, d_reqs: int, d_offsets: int, offsets: np.ndarray, d_table: int, d_stats: int, *,
+                    width: int = 32, persistent: bool = True, stream: int = 0) -> None:
+        """Serve a batched request stream (see gal_run_batches); `offsets` is
+        the host copy of the batch offsets."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        _check(load().gal_run_batches(self.handle, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1, d_table,
+                                      width, 1 if persistent else 0, d_stats, stream))
+
+    def capture_batches(self, d_reqs: int, d_offsets: int, offsets: np.ndarray, d_table: int, d_stats: int, *,
+                        width: int = 32, persistent: bool = True) -> "Graph":
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        g = c_void_p()
+        _check(load().gal_capture_batches(self.handle, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1,
+                                          d_table, width, 1 if persistent else 0, d_stats, ctypes.byref(g)))
+        return Graph(g.value)
+
+    def run_batches_host(self, reqs: np.ndarray, offsets: np.ndarray, table_slots: int, *, width: int = 32,
+                         persistent: bool = True, stream: int = 0, reqs_ptr: int | None = None) -> np.ndarray:
+        """End to end from host buffers; returns the 8 stats words."""
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        out = np.zeros(8, dtype=np.uint64)
+        ptr = reqs_ptr if reqs_ptr is not None else np.ascontiguousarray(reqs, dtype=np.uint64).ctypes.data
+        _check(load().gal_run_batches_host(self.handle, ptr, offsets.ctypes.data, len(offsets) - 1, table_slots, width,
+                                           1 if persistent else 0, out.ctypes.data, stream))
+        return out
+
     # -- inspection -----------------------------------------------------------
     def stats(self) -> dict:
         s = _Stats()
@@ -421,13 +458,35 @@ class Gallatin:
         return out
 
     def veb_layers(self, tree: int = -1, kind: str = "sub_tree") -> list[np.ndarray]:
-        """All layers (top first) of the segment tree (tree=-1), or of sub tree /
-        adoptable-block tree `tree` (kind "sub_tree" or "adopt_tree")."""
+        """All layers (top first) of the segment tree (tree=-1), of sub tree
+        `tree` (kind "sub_tree"), or of slot class `tree`'s adoptable-block or
+        roomy-block tree (kind "adopt_tree" or "roomy_tree")."""
         if tree < 0:
             kind = "segment_tree"
         which = DUMP[kind][0]
         n = load().gal_veb_layer_count(self.handle, which, max(tree, 0))
         return [self.dump(kind, max(tree, 0), i) for i in range(n)]
+
+
+class Graph:
+    """An instantiated CUDA graph owned by the library (gal_capture_batches)."""
+
+    def __init__(self, handle: int):
+        self._g = handle
+
+    def launch(self, stream: int = 0) -> None:
+        _check(load().gal_graph_launch(self._g, stream))
+
+    def close(self) -> None:
+        if self._g:
+            _check(load().gal_graph_destroy(self._g))
+            self._g = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class VebTree:

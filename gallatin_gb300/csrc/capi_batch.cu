@@ -1,0 +1,142 @@
+// C ABI: batched request streams (the batching configuration): one launch per
+// batch, or one cooperative persistent launch over all batches, optionally
+// captured once into a CUDA graph and replayed.
+#include <cuda_runtime.h>
+
+#include "capi_internal.h"
+#include "device_alloc.cuh"
+#include "workloads.cuh"
+
+namespace {
+
+constexpr unsigned kBatchBlock = 256;
+
+int launch_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
+                   uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode, unsigned long long *d_stats,
+                   cudaStream_t s) {
+  gal_device_alloc *a = reinterpret_cast<gal_device_alloc *>(h->d_state);
+  if (mode == 0) {
+    for (uint32_t b = 0; b < n_batches; ++b) {
+      const uint64_t n = h_offsets[b + 1] - h_offsets[b];
+      if (n == 0) continue;
+      galwork::batch_kernel<gal_device_alloc><<<galcapi::grid_for(n, kBatchBlock), kBatchBlock, 0, s>>>(
+          a, d_reqs + h_offsets[b], n, d_table, width, d_stats);
+    }
+    GAL_CUDA_TRY(cudaGetLastError(), "batch launch");
+    return GAL_OK;
+  }
+  int per_sm = 0;
+  GAL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &per_sm, galwork::persistent_batches_kernel<gal_device_alloc>, kBatchBlock, 0),
+               "occupancy query");
+  if (per_sm < 1) return galcapi::fail_invalid("persistent batch kernel does not fit on an SM");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(per_sm * h->hs.num_sms);
+  cfg.blockDim = dim3(kBatchBlock);
+  cfg.stream = s;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  GAL_CUDA_TRY(cudaLaunchKernelEx(&cfg, galwork::persistent_batches_kernel<gal_device_alloc>, a, d_reqs, d_offsets,
+                                  n_batches, d_table, width, d_stats),
+               "persistent batch launch");
+  return GAL_OK;
+}
+
+bool valid_width(uint32_t w) { return w == 8 || w == 16 || w == 32; }
+
+}  // namespace
+
+extern "C" int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets,
+                               const uint64_t *h_offsets, uint32_t n_batches, uint64_t *d_table, uint32_t width,
+                               uint32_t mode, unsigned long long *d_stats, void *stream) {
+  if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
+      d_stats == nullptr)
+    return galcapi::fail_invalid("NULL argument");
+  if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
+  if (mode > 1) return galcapi::fail_invalid("mode must be 0 (per batch) or 1 (persistent)");
+  return launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, d_stats,
+                        (cudaStream_t)stream);
+}
+
+extern "C" int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets,
+                                   const uint64_t *h_offsets, uint32_t n_batches, uint64_t *d_table, uint32_t width,
+                                   uint32_t mode, unsigned long long *d_stats, void **graph_out) {
+  if (graph_out == nullptr) return galcapi::fail_invalid("graph_out is NULL");
+  *graph_out = nullptr;
+  if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
+      d_stats == nullptr)
+    return galcapi::fail_invalid("NULL argument");
+  if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
+  if (mode > 1) return galcapi::fail_invalid("mode must be 0 (per batch) or 1 (persistent)");
+  cudaStream_t s;
+  GAL_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "capture stream");
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  int rc = GAL_OK;
+  if (e == cudaSuccess) {
+    rc = launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, d_stats, s);
+    cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (rc == GAL_OK && e2 != cudaSuccess) rc = galcapi::fail_cuda(e2, "end capture");
+  } else {
+    rc = galcapi::fail_cuda(e, "begin capture");
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (rc == GAL_OK) {
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) rc = galcapi::fail_cuda(e, "graph instantiate");
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(s);
+  if (rc == GAL_OK) *graph_out = exec;
+  return rc;
+}
+
+extern "C" int gal_graph_launch(void *graph_exec, void *stream) {
+  if (graph_exec == nullptr) return galcapi::fail_invalid("graph is NULL");
+  GAL_CUDA_TRY(cudaGraphLaunch((cudaGraphExec_t)graph_exec, (cudaStream_t)stream), "graph launch");
+  return GAL_OK;
+}
+
+extern "C" int gal_graph_destroy(void *graph_exec) {
+  if (graph_exec == nullptr) return GAL_OK;
+  GAL_CUDA_TRY(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec), "graph destroy");
+  return GAL_OK;
+}
+
+namespace {
+int grow(void **p, uint64_t *have, uint64_t need, const char *what) {
+  if (need <= *have) return GAL_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  GAL_CUDA_TRY(cudaMalloc(p, need), what);
+  *have = need;
+  return GAL_OK;
+}
+}  // namespace
+
+extern "C" int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_t *h_offsets,
+                                    uint32_t n_batches, uint64_t table_slots, uint32_t width, uint32_t mode,
+                                    uint64_t *h_stats, void *stream) {
+  if (h == nullptr || h_reqs == nullptr || h_offsets == nullptr || h_stats == nullptr)
+    return galcapi::fail_invalid("NULL argument");
+  const uint64_t nreq = h_offsets[n_batches];
+  int rc;
+  if ((rc = grow((void **)&h->d_breqs, &h->d_breqs_bytes, nreq * 8 + 8, "cudaMalloc batch requests")) ||
+      (rc = grow((void **)&h->d_boffs, &h->d_boffs_bytes, (n_batches + 1) * 8ull, "cudaMalloc batch offsets")) ||
+      (rc = grow((void **)&h->d_btable, &h->d_btable_bytes, table_slots * 8 + 8, "cudaMalloc batch table")))
+    return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  GAL_CUDA_TRY(cudaMemsetAsync(h->d_stats, 0, 64, s), "stats reset");
+  GAL_CUDA_TRY(cudaMemcpyAsync(h->d_breqs, h_reqs, nreq * 8, cudaMemcpyHostToDevice, s), "requests H2D");
+  GAL_CUDA_TRY(cudaMemcpyAsync(h->d_boffs, h_offsets, (n_batches + 1) * 8ull, cudaMemcpyHostToDevice, s),
+               "offsets H2D");
+  rc = gal_run_batches(h, h->d_breqs, h->d_boffs, h_offsets, n_batches, h->d_btable, width, mode, h->d_stats, stream);
+  if (rc != GAL_OK) return rc;
+  GAL_CUDA_TRY(cudaMemcpyAsync(h_stats, h->d_stats, 64, cudaMemcpyDeviceToHost, s), "stats D2H");
+  GAL_CUDA_TRY(cudaStreamSynchronize(s), "batch e2e sync");
+  return GAL_OK;
+}

@@ -123,6 +123,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   h->d_classes = nullptr;
   h->d_classes_bytes = 0;
   h->d_stats = nullptr;
+  h->d_breqs = h->d_boffs = h->d_btable = nullptr;
+  h->d_breqs_bytes = h->d_boffs_bytes = h->d_btable_bytes = 0;
   h->min_size = min_size;
   h->max_size = max_size;
   gal_state_t &s = h->hs;
@@ -137,22 +139,30 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   s.block_shift_min = min_shift + 12;
   s.blocks_per_segment = (uint32_t)(segment_bytes >> s.block_shift_min);
   s.seg_block_words = (s.blocks_per_segment + 63) / 64;
-  s.ext_blocks_per_segment = s.blocks_per_segment >> (num_trees - 1);
+  // the largest tree serves runs of 1, 2, 4 ... slices up to half the
+  // smallest block (min_size << 11 bytes), one slot class per run length
+  const int max_run = 12 - num_trees > 0 ? 12 - num_trees : 0;
+  s.num_classes = (uint32_t)(num_trees + max_run);
   s.num_sms = (uint32_t)prop.multiProcessorCount;
   s.seed = seed;
-  // Pinned blocks per size class: one per SM for small classes; for large
-  // classes as many as a quarter of the arena split evenly over the classes
-  // affords (a block of class t is 4096 slices of min << t bytes).
+  // Pinned blocks per slot class: one per SM for small trees; for large
+  // trees as many as a quarter of the arena split evenly over the trees
+  // affords (a block of tree t is 4096 slices of min << t bytes). A run
+  // class of 2^r slices of the largest tree gets that tree's count >> r (at
+  // least 2): its requests are rarer. Slots are filled on first use, so a
+  // class that is never asked for pins nothing.
   if (min_slots == 0) min_slots = 4;
   const uint64_t budget = s.arena_bytes / (4ull * (uint64_t)num_trees);
   uint32_t total = 0;
-  for (int t = 0; t < num_trees; ++t) {
+  for (uint32_t k = 0; k < s.num_classes; ++k) {
+    const int t = (int)k < num_trees ? (int)k : num_trees - 1;
     const uint64_t block_bytes = 4096ull * (min_size << t);
     uint64_t c = budget / block_bytes;
     if (c > s.num_sms) c = s.num_sms;
     if (c < min_slots) c = min_slots;
-    s.slot_count[t] = (uint32_t)c;
-    s.slot_offset[t] = total;
+    if ((int)k >= num_trees) c = (c >> (k - (uint32_t)num_trees + 1)) > 2 ? (c >> (k - (uint32_t)num_trees + 1)) : 2;
+    s.slot_count[k] = (uint32_t)c;
+    s.slot_offset[k] = total;
     total += (uint32_t)c;
   }
   s.total_slots = total;
@@ -171,8 +181,6 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
     return cleanup(rc);
   if ((rc = device_alloc(h, &s.block_meta, nblocks, "cudaMalloc block_meta")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.block_bits, nblocks * 64, "cudaMalloc block_bits")) != GAL_OK) return cleanup(rc);
-  const uint64_t next = num_segments * s.ext_blocks_per_segment;
-  if ((rc = device_alloc(h, &s.block_ext, next * 64, "cudaMalloc block_ext")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.slots, total, "cudaMalloc slots")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.locks, 1, "cudaMalloc locks")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.counters, GAL_NUM_COUNTERS, "cudaMalloc counters")) != GAL_OK) return cleanup(rc);
@@ -186,7 +194,6 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
       (rc = try_cuda(cudaMemset(s.seg_block_bits, 0, num_segments * s.seg_block_words * 8), "memset seg bits")) ||
       (rc = try_cuda(cudaMemset(s.block_meta, 0, nblocks * 8), "memset block_meta")) ||
       (rc = try_cuda(cudaMemset(s.block_bits, 0, nblocks * 64 * 8), "memset block_bits")) ||
-      (rc = try_cuda(cudaMemset(s.block_ext, 0, next * 64 * 8), "memset block_ext")) ||
       (rc = try_cuda(cudaMemset(s.locks, 0, sizeof(uint32_t)), "memset locks")) ||
       (rc = try_cuda(cudaMemset(s.counters, 0, GAL_NUM_COUNTERS * 8), "memset counters")) ||
       (rc = try_cuda(cudaMemset(h->d_stats, 0, 64), "memset stats")))
@@ -208,7 +215,10 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
     if ((rc = galcapi::build_veb(&s.sub_trees[t], num_segments, seed + (uint64_t)t, false, h->device_allocs)) !=
         GAL_OK)
       return cleanup(rc);
-    if ((rc = galcapi::build_veb(&s.adopt_trees[t], nblocks, seed + (uint64_t)t, false, h->device_allocs)) != GAL_OK)
+  }
+  for (uint32_t k = 0; k < s.num_classes; ++k) {
+    if ((rc = galcapi::build_veb(&s.adopt_trees[k], nblocks, seed + k, false, h->device_allocs)) != GAL_OK ||
+        (rc = galcapi::build_veb(&s.roomy_trees[k], nblocks, seed + 0x100 + k, false, h->device_allocs)) != GAL_OK)
       return cleanup(rc);
   }
   if ((rc = device_alloc(h, &h->d_state, 1, "cudaMalloc state")) != GAL_OK) return cleanup(rc);
@@ -231,6 +241,9 @@ extern "C" int gal_destroy(gal_allocator *h) {
     g_registry.erase(h->d_state);
   }
   if (h->d_classes) cudaFree(h->d_classes);
+  if (h->d_breqs) cudaFree(h->d_breqs);
+  if (h->d_boffs) cudaFree(h->d_boffs);
+  if (h->d_btable) cudaFree(h->d_btable);
   free_all(h->device_allocs);
   delete h;
   if (e != cudaSuccess) return galcapi::fail_cuda(e, "destroy sync");
@@ -258,7 +271,8 @@ extern "C" int gal_geometry(gal_allocator *h, gal_geometry_t *out) {
   out->blocks_per_segment = s.blocks_per_segment;
   out->num_sms = s.num_sms;
   out->total_slots = s.total_slots;
-  for (int t = 0; t < s.num_trees; ++t) out->slot_count[t] = s.slot_count[t];
+  out->num_classes = s.num_classes;
+  for (uint32_t k = 0; k < s.num_classes; ++k) out->slot_count[k] = s.slot_count[k];
   out->arena_base = (uint64_t)s.memory;
   return GAL_OK;
 }
@@ -266,9 +280,10 @@ extern "C" int gal_geometry(gal_allocator *h, gal_geometry_t *out) {
 extern "C" int gal_veb_layer_count(gal_allocator *h, int which, int tree) {
   if (h == nullptr) return -1;
   if (which == GAL_DUMP_SEGMENT_TREE) return h->hs.segment_tree.num_layers;
-  if (tree < 0 || tree >= h->hs.num_trees) return -1;
-  if (which == GAL_DUMP_SUB_TREE) return h->hs.sub_trees[tree].num_layers;
+  if (which == GAL_DUMP_SUB_TREE) return (tree >= 0 && tree < h->hs.num_trees) ? h->hs.sub_trees[tree].num_layers : -1;
+  if (tree < 0 || tree >= (int)h->hs.num_classes) return -1;
   if (which == GAL_DUMP_ADOPT_TREE) return h->hs.adopt_trees[tree].num_layers;
+  if (which == GAL_DUMP_ROOMY_TREE) return h->hs.roomy_trees[tree].num_layers;
   return -1;
 }
 
@@ -281,17 +296,18 @@ static bool dump_source(gal_allocator *h, int which, int tree, int layer, const 
     case GAL_DUMP_SEG_BLOCK_BITS: *src = s.seg_block_bits; *bytes = s.num_segments * s.seg_block_words * 8; return true;
     case GAL_DUMP_BLOCK_META: *src = s.block_meta; *bytes = nblocks * 8; return true;
     case GAL_DUMP_BLOCK_BITS: *src = s.block_bits; *bytes = nblocks * 64 * 8; return true;
-    case GAL_DUMP_BLOCK_EXT: *src = s.block_ext; *bytes = s.num_segments * s.ext_blocks_per_segment * 64 * 8; return true;
     case GAL_DUMP_SLOTS: *src = s.slots; *bytes = (uint64_t)s.total_slots * 8; return true;
     case GAL_DUMP_COUNTERS: *src = s.counters; *bytes = GAL_NUM_COUNTERS * 8; return true;
     case GAL_DUMP_LOCKS: *src = s.locks; *bytes = 4; return true;
     case GAL_DUMP_SEGMENT_TREE:
     case GAL_DUMP_SUB_TREE:
-    case GAL_DUMP_ADOPT_TREE: {
+    case GAL_DUMP_ADOPT_TREE:
+    case GAL_DUMP_ROOMY_TREE: {
       const gal_veb_t *t = nullptr;
       if (which == GAL_DUMP_SEGMENT_TREE) t = &s.segment_tree;
-      else if (tree >= 0 && tree < s.num_trees)
-        t = (which == GAL_DUMP_SUB_TREE) ? &s.sub_trees[tree] : &s.adopt_trees[tree];
+      else if (which == GAL_DUMP_SUB_TREE && tree >= 0 && tree < s.num_trees) t = &s.sub_trees[tree];
+      else if (which == GAL_DUMP_ADOPT_TREE && tree >= 0 && tree < (int)s.num_classes) t = &s.adopt_trees[tree];
+      else if (which == GAL_DUMP_ROOMY_TREE && tree >= 0 && tree < (int)s.num_classes) t = &s.roomy_trees[tree];
       if (t == nullptr || layer < 0 || layer >= t->num_layers) return false;
       *src = t->bits[layer];
       *bytes = t->layer_words[layer] * 8;
@@ -384,7 +400,7 @@ extern "C" int gal_print_info(gal_allocator *h) {
          (unsigned long long)st.segments_in_allocations);
   const uint64_t nblocks = s.num_segments * s.blocks_per_segment;
   uint64_t overhead = sizeof(gal_state_t) + s.num_segments * (2 + 4 + 8ull * s.seg_block_words) +
-                      nblocks * (8 + 512) + s.num_segments * s.ext_blocks_per_segment * 512 + s.total_slots * 8ull;
+                      nblocks * (8 + 512) + s.total_slots * 8ull;
   printf("Allocator is using %llu bytes of overhead\n", (unsigned long long)overhead);
   printf("Counters: oom slice %llu block %llu segment %llu, timeouts %llu, bad frees %llu, corrupt %llu\n",
          (unsigned long long)st.counters[GAL_CTR_OOM_SLICE], (unsigned long long)st.counters[GAL_CTR_OOM_BLOCK],

@@ -19,6 +19,13 @@ struct gal_allocator {
   uint8_t *d_classes;
   uint64_t d_classes_bytes;
   unsigned long long *d_stats;
+  // scratch of the host-buffer batch entry point, grown on demand
+  uint64_t *d_breqs;
+  uint64_t d_breqs_bytes;
+  uint64_t *d_boffs;
+  uint64_t d_boffs_bytes;
+  uint64_t *d_btable;
+  uint64_t d_btable_bytes;
 };
 
 struct gal_veb {

@@ -3,18 +3,10 @@
 #include <cuda_runtime.h>
 
 #include "capi_internal.h"
-#include "gallatin_gb300/alloc.cuh"
+#include "device_alloc.cuh"
 #include "workloads.cuh"
 
 namespace {
-
-// The device allocator seen through the malloc/free interface the workload
-// templates expect; same layout as gal_state_t.
-struct gal_device_alloc {
-  gal_state_t state;
-  __device__ __forceinline__ void *malloc(uint64_t n) { return gal::malloc(&state, n); }
-  __device__ __forceinline__ void free(void *p) { gal::free(&state, p); }
-};
 
 __global__ void malloc_batch_kernel(const gal_state_t *st, const uint64_t *sizes, uint64_t n, uint64_t *out) {
   const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;

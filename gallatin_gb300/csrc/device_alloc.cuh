@@ -1,0 +1,16 @@
+// The device allocator seen through the malloc/free interface the workload
+// templates (workloads.cuh) expect; same layout as gal_state_t.
+#ifndef GALLATIN_GB300_DEVICE_ALLOC_CUH
+#define GALLATIN_GB300_DEVICE_ALLOC_CUH
+
+#include "gallatin_gb300/alloc.cuh"
+
+struct gal_device_alloc {
+  gal_state_t state;
+  __device__ __forceinline__ void *malloc(uint64_t n) { return gal::malloc(&state, n); }
+  __device__ __forceinline__ void free(void *p) { gal::free(&state, p); }
+  __device__ __forceinline__ void *malloc_w(uint64_t n, uint32_t w) { return gal::malloc(&state, n, w); }
+  __device__ __forceinline__ void free_w(void *p, uint32_t w) { gal::free(&state, p, w); }
+};
+
+#endif  // GALLATIN_GB300_DEVICE_ALLOC_CUH

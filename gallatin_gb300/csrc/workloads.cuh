@@ -20,6 +20,7 @@
 #ifndef GALLATIN_GB300_WORKLOADS_CUH
 #define GALLATIN_GB300_WORKLOADS_CUH
 
+#include <cooperative_groups.h>
 #include <stdint.h>
 
 // CTAs per SM the mixed workload kernel is compiled for (0: compiler's
@@ -137,6 +138,76 @@ __global__ void GALWORK_MIXED_BOUNDS mixed_kernel(Alloc *alloc, uint64_t n, uint
   }
   if (misses) atomicAdd(stats + STAT_MISS, misses);
   if (bad) atomicAdd(stats + STAT_BAD, bad);
+}
+
+// ---- batched request streams -------------------------------------------
+//
+// A request is one u64: the high 32 bits name a slot of the live-set table,
+// the low 32 bits are a size. size > 0: table[slot] = malloc(size); size 0:
+// free(table[slot]). The host generator only frees slots filled by an
+// earlier batch, so the requests of one batch are independent.
+
+// malloc/free with an aggregation width when the allocator offers one
+template <class A>
+__device__ __forceinline__ auto wl_malloc(A *a, uint64_t s, uint32_t w, int) -> decltype(a->malloc_w(s, w)) {
+  return a->malloc_w(s, w);
+}
+template <class A>
+__device__ __forceinline__ void *wl_malloc(A *a, uint64_t s, uint32_t, long) {
+  return a->malloc(s);
+}
+template <class A>
+__device__ __forceinline__ auto wl_free(A *a, void *p, uint32_t w, int) -> decltype(a->free_w(p, w)) {
+  return a->free_w(p, w);
+}
+template <class A>
+__device__ __forceinline__ void wl_free(A *a, void *p, uint32_t, long) {
+  a->free(p);
+}
+
+template <class A>
+__device__ __forceinline__ void serve_request(A *a, uint64_t req, uint64_t *table, uint32_t width,
+                                              unsigned long long &misses) {
+  const uint32_t slot = (uint32_t)(req >> 32);
+  const uint32_t size = (uint32_t)req;
+  if (size != 0) {
+    void *p = wl_malloc(a, size, width, 0);
+    if (p == nullptr) ++misses;
+    table[slot] = (uint64_t)p;
+  } else {
+    void *p = (void *)table[slot];
+    if (p != nullptr) wl_free(a, p, width, 0);  // a malloc that failed left 0
+    table[slot] = 0;
+  }
+}
+
+// plain path: one launch per batch, one thread per request
+template <class A>
+__global__ void batch_kernel(A *a, const uint64_t *reqs, uint64_t n, uint64_t *table, uint32_t width,
+                             unsigned long long *stats) {
+  const uint64_t i = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
+  unsigned long long misses = 0;
+  if (i < n) serve_request(a, reqs[i], table, width, misses);
+  if (misses) atomicAdd(stats + STAT_MISS, misses);
+}
+
+// persistent path: every batch in one cooperative launch; the grid syncs
+// between batches (which also orders a batch's table writes before the next
+// batch's frees read them)
+template <class A>
+__global__ void persistent_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets, uint32_t n_batches,
+                                          uint64_t *table, uint32_t width, unsigned long long *stats) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t rank = grid.thread_rank();
+  unsigned long long misses = 0;
+  for (uint32_t b = 0; b < n_batches; ++b) {
+    const uint64_t hi = offsets[b + 1];
+    for (uint64_t i = offsets[b] + rank; i < hi; i += nthreads) serve_request(a, reqs[i], table, width, misses);
+    grid.sync();
+  }
+  if (misses) atomicAdd(stats + STAT_MISS, misses);
 }
 
 }  // namespace galwork

@@ -42,7 +42,11 @@ typedef struct gal_geometry_t {
   uint32_t blocks_per_segment;
   uint32_t num_sms;
   uint32_t total_slots;
-  uint32_t slot_count[GAL_MAX_TREES];
+  uint32_t slot_count[GAL_MAX_TREES]; /* per slot class */
+  uint32_t num_classes;               /* slot classes: num_trees - 1 single-slice
+                                         trees, then one per run length 1, 2, 4 ...
+                                         of the largest tree */
+  uint32_t pad_;
   uint64_t arena_base; /* device address of the arena */
 } gal_geometry_t;
 
@@ -63,9 +67,9 @@ typedef struct gal_stats_t {
  * min_size and max_size must be powers of two with
  * segment_bytes >= max_size * 4096 (reference static_assert gallatin.cuh:300)
  * and max_size >= 32 * min_size (multi-slice runs fit one bitmap word).
- * min_slots: floor on pinned blocks per size class (0 = default 4); the
+ * min_slots: floor on pinned blocks per slot class (0 = default 4); the
  * count per class is otherwise one per SM, capped so a class's pinned blocks
- * take at most a quarter of the arena divided by the number of classes.
+ * take at most a quarter of the arena divided by the number of trees.
  * Replaces Gallatin<seg,min,max>::generate_on_device. */
 int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size, uint64_t max_size,
                uint32_t min_slots, gal_allocator **out);
@@ -98,17 +102,19 @@ int gal_reset_counters(gal_allocator *h);
 #define GAL_DUMP_SEG_BLOCK_BITS 2
 #define GAL_DUMP_BLOCK_META 3
 #define GAL_DUMP_BLOCK_BITS 4
-#define GAL_DUMP_BLOCK_EXT 5
+/* 5 is unused */
 #define GAL_DUMP_SLOTS 6
 #define GAL_DUMP_COUNTERS 7
 #define GAL_DUMP_SEGMENT_TREE 8
 #define GAL_DUMP_SUB_TREE 9
 #define GAL_DUMP_LOCKS 10
 #define GAL_DUMP_ADOPT_TREE 11
+#define GAL_DUMP_ROOMY_TREE 12
 int64_t gal_dump_bytes(gal_allocator *h, int which, int tree, int layer);
 int gal_dump(gal_allocator *h, int which, int tree, int layer, void *host_dst, uint64_t bytes);
 /* layers of a vEB tree of this allocator: which is GAL_DUMP_SEGMENT_TREE,
- * GAL_DUMP_SUB_TREE or GAL_DUMP_ADOPT_TREE (tree selects the size class) */
+ * GAL_DUMP_SUB_TREE (tree selects the size class), GAL_DUMP_ADOPT_TREE or
+ * GAL_DUMP_ROOMY_TREE (tree selects the slot class) */
 int gal_veb_layer_count(gal_allocator *h, int which, int tree);
 
 /* --- batch entry points (device buffers, one thread per request) ---
@@ -159,6 +165,31 @@ int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, ui
 int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
                                uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,
                                uint32_t block_dim, uint64_t *h_stats, void *stream);
+
+/* --- batched request streams (no reference counterpart: the reference only
+ *     serves per-thread calls from user kernels) ---
+ * A request is a u64: slot << 32 | size; size > 0 mallocs into
+ * table[slot], size 0 frees table[slot]. Batch b is requests
+ * [offsets[b], offsets[b+1]). width (8, 16, 32) limits warp aggregation to
+ * tiles of that many lanes. mode 0: one launch per batch (the plain
+ * per-thread call path); mode 1: one cooperative persistent launch that
+ * serves every batch with a grid barrier between batches. stats as for the
+ * workloads ([0] = mallocs that returned NULL). */
+int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
+                    uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode,
+                    unsigned long long *d_stats, void *stream);
+/* Capture the same launches once into an instantiated CUDA graph; replay it
+ * with gal_graph_launch and release it with gal_graph_destroy. */
+int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
+                        uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode,
+                        unsigned long long *d_stats, void **graph_out);
+int gal_graph_launch(void *graph_exec, void *stream);
+int gal_graph_destroy(void *graph_exec);
+/* End to end from host buffers: copies the requests and offsets to scratch
+ * the handle owns (grown on demand), runs, copies the 8 stats words back and
+ * synchronises `stream`. table_slots: size of the live-set table. */
+int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_t *h_offsets, uint32_t n_batches,
+                         uint64_t table_slots, uint32_t width, uint32_t mode, uint64_t *h_stats, void *stream);
 
 /* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
 

@@ -19,8 +19,13 @@
 // bits with fetch-and; frees return bits with fetch-or and release the
 // reservation. Freed slices are reused while the block stays pinned, so a
 // block is replaced only when it is full, and it is recycled to its
-// segment's free-block bitmap when its last slice comes back. Every wait is
-// bounded; exhausted budgets return nullptr and bump a device counter.
+// segment's free-block bitmap when its last slice comes back. A replaced
+// block that still holds slices is detached; once half of it has drained it
+// is pinned again ahead of a fresh block, so long-lived allocations freed in
+// random order do not strand the arena in half-empty blocks. Blocks of the
+// largest tree serve one run length each (1, 2, 4 ... slices) for as long as
+// they are out of their segment, so multi-slice runs never fragment. Every
+// wait is bounded; exhausted budgets return nullptr and bump a device counter.
 #ifndef GALLATIN_GB300_ALLOC_CUH
 #define GALLATIN_GB300_ALLOC_CUH
 
@@ -40,6 +45,11 @@ constexpr int kSegmentLockBit = 31;
 // a pinned block past this many live slices is replaced ahead of time, so
 // warps rarely find their slot's block full
 constexpr uint32_t kRefillMark = GAL_BLOCK_SLICES * 7 / 8;
+constexpr int kAdoptCandidates = 64;
+
+// which detached blocks request_block may pin again
+enum { ADOPT_NONE = 0, ADOPT_ROOMY = 1, ADOPT_ANY = 2 };
+enum { REPLACE_OK = 0, REPLACE_BUSY = 1, REPLACE_NOMEM = 2 };
 
 enum { TIER_SLICE = 0, TIER_BLOCK = 1, TIER_SEGMENT = 2 };
 
@@ -99,6 +109,8 @@ __device__ __forceinline__ size_class classify(const gal_state_t *st, uint64_t s
 __device__ __forceinline__ uint32_t meta_live(uint64_t m) { return (uint32_t)m; }
 __device__ __forceinline__ uint32_t meta_tree(uint64_t m) { return (uint32_t)(m >> GAL_META_TREE_SHIFT) & 0xFFu; }
 __device__ __forceinline__ uint32_t meta_state(uint64_t m) { return (uint32_t)(m >> GAL_META_STATE_SHIFT) & 3u; }
+__device__ __forceinline__ uint32_t meta_run(uint64_t m) { return (uint32_t)(m >> GAL_META_RUN_SHIFT) & 0xFu; }
+__device__ __forceinline__ uint32_t meta_class(uint64_t m) { return meta_tree(m) + meta_run(m); }
 __device__ __forceinline__ uint32_t meta_cursor(uint64_t m) { return (uint32_t)(m >> GAL_META_CURSOR_SHIFT); }
 
 __device__ __forceinline__ void count(const gal_state_t *st, int id) {
@@ -114,13 +126,6 @@ __device__ __forceinline__ char *block_address(const gal_state_t *st, uint64_t b
   const uint64_t seg = b >> bis;
   const uint64_t i = b & ((1ull << bis) - 1);
   return st->memory + (seg << st->segment_shift) + (i << (st->block_shift_min + (int)t));
-}
-
-__device__ __forceinline__ uint64_t *ext_words(const gal_state_t *st, uint64_t b) {
-  const int bis = block_index_shift(st);
-  const uint64_t seg = b >> bis;
-  const uint64_t i = b & ((1ull << bis) - 1);
-  return st->block_ext + ((seg * st->ext_blocks_per_segment + i) << 6);
 }
 
 // Aligned runs of c (a power of two <= 64) free bits: bit j is set when bits
@@ -285,37 +290,46 @@ __device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b
   count(st, GAL_CTR_BLOCK_RETIRE);
 }
 
-// A block belongs in adoptable tree t exactly while it is DETACHED and
-// formatted for t (same apply-then-confirm discipline as sub_tree_sync).
-__device__ inline void adopt_sync(const gal_state_t *st, uint32_t t, uint64_t b) {
-  const gal_veb_t *at = &st->adopt_trees[t];
-  auto listed = [&]() {
-    const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
-    return meta_state(m) == GAL_STATE_DETACHED && meta_tree(m) == t;
-  };
-  bool want = listed();
+// A block belongs in class k's adoptable tree exactly while it is DETACHED
+// and serves class k, and in class k's roomy tree while in addition its live
+// count is at most GAL_ROOMY_MARK (same apply-then-confirm discipline as
+// sub_tree_sync: the last change to the facts is always applied).
+__device__ __forceinline__ bool adopt_listed(uint64_t m, uint32_t k, bool roomy) {
+  return meta_state(m) == GAL_STATE_DETACHED && meta_class(m) == k && (!roomy || meta_live(m) <= GAL_ROOMY_MARK);
+}
+
+__device__ inline void adopt_sync(const gal_state_t *st, uint32_t k, uint64_t b, bool roomy) {
+  const gal_veb_t *at = roomy ? &st->roomy_trees[k] : &st->adopt_trees[k];
+  bool want = adopt_listed(ptx::ld_relaxed(st->block_meta + b), k, roomy);
   for (int i = 0; i < 8; ++i) {
     if (want) {
       veb::insert_force_update(at, b);
     } else {
       veb::remove(at, b);
     }
-    const bool now = listed();
+    const bool now = adopt_listed(ptx::ld_relaxed(st->block_meta + b), k, roomy);
     if (now == want) return;
     want = now;
   }
 }
 
-// A DETACHED block whose live count reached zero goes back to its segment.
+__device__ __forceinline__ void adopt_sync_both(const gal_state_t *st, uint32_t k, uint64_t b) {
+  adopt_sync(st, k, b, false);
+  adopt_sync(st, k, b, true);
+}
+
+// A DETACHED block whose live count reached zero, or a block-tier (WHOLE)
+// block whose allocation was freed, goes back to its segment.
 __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
   uint64_t *mp = st->block_meta + b;
   uint64_t m = ptx::ld_relaxed(mp);
   for (int i = 0; i < 64; ++i) {
-    if (meta_state(m) != GAL_STATE_DETACHED || meta_live(m) != 0) return;
-    const uint64_t nm = m - ((uint64_t)GAL_STATE_DETACHED << GAL_META_STATE_SHIFT);
+    const uint32_t state = meta_state(m);
+    if ((state != GAL_STATE_DETACHED && state != GAL_STATE_WHOLE) || meta_live(m) != 0) return;
+    const uint64_t nm = m - ((uint64_t)state << GAL_META_STATE_SHIFT);
     const uint64_t r = ptx::cas_acq_rel(mp, m, nm);
     if (r == m) {
-      adopt_sync(st, meta_tree(m), b);
+      if (state == GAL_STATE_DETACHED) adopt_sync_both(st, meta_class(m), b);
       return_block_to_segment(st, b);
       return;
     }
@@ -325,18 +339,26 @@ __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
 
 __device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n) {
   const uint64_t old = ptx::atom_add_release(st->block_meta + b, (uint64_t)(-(int64_t)n));
-  if (meta_state(old) == GAL_STATE_DETACHED && meta_live(old) == n) try_retire_block(st, b);
+  const uint32_t state = meta_state(old);
+  const uint32_t live = meta_live(old);
+  if ((state == GAL_STATE_DETACHED || state == GAL_STATE_WHOLE) && live == n) {
+    try_retire_block(st, b);
+  } else if (state == GAL_STATE_DETACHED && live > GAL_ROOMY_MARK && live - n <= GAL_ROOMY_MARK) {
+    adopt_sync(st, meta_class(old), b, true);
+  }
 }
 
-// Move a block this thread owns from FREE to `state` formatted for t,
-// adding `live` to its live count.
-__device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t state,
-                                          uint32_t live) {
+// Move a block this thread owns from FREE to `state`, formatted for tree t
+// and run length 2^r, adding `live` to its live count.
+__device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r,
+                                          uint32_t state, uint32_t live) {
   const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
   const int64_t dstate = (int64_t)state - (int64_t)meta_state(m);
   const int64_t dtree = (int64_t)t - (int64_t)meta_tree(m);
+  const int64_t drun = (int64_t)r - (int64_t)meta_run(m);
   const uint64_t delta = (uint64_t)(dstate * (1ll << GAL_META_STATE_SHIFT)) +
-                         (uint64_t)(dtree * (1ll << GAL_META_TREE_SHIFT)) + (uint64_t)live;
+                         (uint64_t)(dtree * (1ll << GAL_META_TREE_SHIFT)) +
+                         (uint64_t)(drun * (1ll << GAL_META_RUN_SHIFT)) + (uint64_t)live;
   ptx::atom_add_release(st->block_meta + b, delta);
 }
 
@@ -344,75 +366,99 @@ __device__ __forceinline__ uint64_t mix_tid(uint64_t tid, int attempt) {
   return attempt == 0 ? tid : murmur64a_u64(tid, (uint64_t)attempt);
 }
 
-// Pin again a DETACHED block of tree t that still has room (used only when no
-// fresh block can be had). The block keeps its live slices and bitmap.
-__device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t t) {
-  const gal_veb_t *at = &st->adopt_trees[t];
-  uint64_t cand = veb::find_first_valid_index(at);
-  for (int k = 0; k < 64 && cand != veb::kFail; ++k) {
+__device__ __forceinline__ bool veb_maybe_nonempty(const gal_veb_t *v) {
+  for (uint64_t w = 0; w < v->layer_words[0]; ++w)
+    if (ptx::ld_relaxed(v->bits[0] + w)) return true;
+  return false;
+}
+
+// Pin again a DETACHED block of class k (tree t, run length c slices): from
+// the roomy tree (live <= GAL_ROOMY_MARK), or from the adoptable tree any
+// block with room for one more run. The block keeps its live slices and its
+// bitmap. Candidates are visited from a hashed start so that concurrent
+// adopters spread out.
+__device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32_t c, uint64_t tid, bool roomy) {
+  const gal_veb_t *at = roomy ? &st->roomy_trees[k] : &st->adopt_trees[k];
+  if (!veb_maybe_nonempty(at)) return GAL_EMPTY_BLOCK;
+  const uint64_t start = murmur64a_u64(tid, at->seed) % at->universe;
+  uint64_t cand = veb::query(at, start) ? start : veb::successor_thorough(at, start);
+  bool wrapped = false;
+  for (int n = 0; n < kAdoptCandidates; ++n) {
+    if (cand == veb::kFail) {
+      if (wrapped) break;
+      wrapped = true;
+      cand = veb::find_first_valid_index(at);
+      if (cand == veb::kFail) break;
+    }
     uint64_t m = ptx::ld_relaxed(st->block_meta + cand);
     for (int i = 0; i < 8; ++i) {
-      if (meta_state(m) != GAL_STATE_DETACHED || meta_tree(m) != t || meta_live(m) >= GAL_BLOCK_SLICES) break;
+      if (!adopt_listed(m, k, roomy) || meta_live(m) + c > GAL_BLOCK_SLICES) break;
       const uint64_t nm = m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
       const uint64_t r = ptx::cas_acq_rel(st->block_meta + cand, m, nm);
       if (r == m) {
-        adopt_sync(st, t, cand);
-        count(st, GAL_CTR_ADOPT);
+        adopt_sync_both(st, k, cand);
+        count(st, roomy ? GAL_CTR_ADOPT_ROOMY : GAL_CTR_ADOPT);
         return (uint32_t)cand;
       }
       m = r;
     }
-    if (meta_state(m) != GAL_STATE_DETACHED || meta_tree(m) != t) adopt_sync(st, t, cand);
+    if (!adopt_listed(m, k, roomy)) adopt_sync(st, k, cand, roomy);
     cand = veb::successor_thorough(at, cand);
   }
   return GAL_EMPTY_BLOCK;
 }
 
-// A FREE block of tree t, from a segment already formatted for t or from a
-// newly attached one. When the arena has neither and allow_adopt is set, a
-// DETACHED block with room is pinned again instead (*adopted = true; it is
-// already PINNED). GAL_EMPTY_BLOCK when nothing can be had.
-__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint64_t tid, bool allow_adopt,
-                                         bool *adopted) {
+// A block for slot class k (tree t, run length c): with adopt_mode >=
+// ADOPT_ROOMY first a detached block of the class that drained to half or
+// less; then a FREE block from a segment already formatted for t or from a
+// newly attached one; with ADOPT_ANY, when the arena has neither, a detached
+// block with any room. An adopted block is already PINNED (*adopted = true).
+// GAL_EMPTY_BLOCK when nothing can be had.
+__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint32_t k, uint32_t c, uint64_t tid,
+                                         int adopt_mode, bool *adopted) {
   *adopted = false;
+  if (adopt_mode >= ADOPT_ROOMY) {
+    const uint32_t b = adopt_block(st, k, c, tid, true);
+    if (b != GAL_EMPTY_BLOCK) {
+      *adopted = true;
+      return b;
+    }
+  }
   const gal_veb_t *sub = &st->sub_trees[t];
-  for (int a = 0; a < kRequestBlockAttempts; ++a) {
+  int a = 0;
+  for (; a < kRequestBlockAttempts; ++a) {
     uint64_t seg = veb::find_random_valid_index(sub, mix_tid(tid, a));
     if (seg == veb::kFail) {
-      if (try_lock(st, (int)t)) {
-        seg = attach_segment(st, t);
-        unlock(st, (int)t);
-        if (seg == veb::kFail) {
-          if (veb::find_first_valid_index(sub) != veb::kFail) continue;
-          if (!allow_adopt) return GAL_EMPTY_BLOCK;
-          const uint32_t b = adopt_block(st, t);
-          *adopted = b != GAL_EMPTY_BLOCK;
-          return b;
-        }
-      } else {
+      if (!try_lock(st, (int)t)) {
         backoff(a);
         continue;
+      }
+      seg = attach_segment(st, t);
+      unlock(st, (int)t);
+      if (seg == veb::kFail) {
+        if (veb::find_first_valid_index(sub) != veb::kFail) continue;
+        break;  // no formatted segment with a free block, no free segment
       }
     }
     const uint32_t b = take_block(st, seg, t);
     if (b != GAL_EMPTY_BLOCK) return b;
   }
-  count(st, GAL_CTR_TIMEOUT);
+  if (a == kRequestBlockAttempts) count(st, GAL_CTR_TIMEOUT);
+  if (adopt_mode == ADOPT_ANY) {
+    const uint32_t b = adopt_block(st, k, c, tid, false);
+    *adopted = b != GAL_EMPTY_BLOCK;
+    return b;
+  }
   return GAL_EMPTY_BLOCK;
 }
 
 // ---- pinned blocks -------------------------------------------------------
 
-__device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t) {
+__device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r) {
   ulonglong2 *bits = reinterpret_cast<ulonglong2 *>(st->block_bits + (b << 6));
   const ulonglong2 ones = make_ulonglong2(~0ull, ~0ull);
   for (int i = 0; i < 32; ++i) bits[i] = ones;
-  if (t == (uint32_t)st->num_trees - 1) {
-    ulonglong2 *ext = reinterpret_cast<ulonglong2 *>(ext_words(st, b));
-    const ulonglong2 zero = make_ulonglong2(0ull, 0ull);
-    for (int i = 0; i < 32; ++i) ext[i] = zero;
-  }
-  own_block(st, b, t, GAL_STATE_PINNED, 0);  // release: bitmap before PINNED
+  own_block(st, b, t, r, GAL_STATE_PINNED, 0);  // release: bitmap before PINNED
   count(st, GAL_CTR_BLOCK_PINS);
   count(st, GAL_CTR_TREE_PINS + (int)t);
 }
@@ -423,44 +469,60 @@ __device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) 
   if (meta_live(old) == 0) {
     try_retire_block(st, b);
   } else {
-    adopt_sync(st, meta_tree(old), b);
+    adopt_sync(st, meta_class(old), b, false);
+    // a release that crossed the mark before the detach could not list it
+    if (meta_live(old) <= GAL_ROOMY_MARK) adopt_sync(st, meta_class(old), b, true);
   }
 }
 
-// Replace the block a slot holds (`seen`, without the REPLACING flag) by a
-// freshly pinned one. Only the thread whose CAS sets REPLACING does the work.
-__device__ inline uint32_t replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t,
-                                        uint64_t tid, bool allow_adopt = true) {
-  if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return GAL_EMPTY_BLOCK;
+// Replace the block a slot holds (`seen`, without the REPLACING flag) by
+// another pinned one. Only the thread whose CAS sets REPLACING does the work;
+// REPLACE_NOMEM when request_block found nothing (the slot is left as seen).
+__device__ inline int replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t, uint32_t r,
+                                   uint64_t tid, int adopt_mode, uint32_t *out) {
+  *out = GAL_EMPTY_BLOCK;
+  if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return REPLACE_BUSY;
   bool adopted = false;
-  const uint32_t nb = request_block(st, t, tid, allow_adopt, &adopted);
+  const uint32_t nb = request_block(st, t, t + r, 1u << r, tid, adopt_mode, &adopted);
   if (nb == GAL_EMPTY_BLOCK) {
     ptx::st_release(slot, seen);
-    return GAL_EMPTY_BLOCK;
+    return REPLACE_NOMEM;
   }
-  if (!adopted) pin_block(st, nb, t);
+  if (!adopted) pin_block(st, nb, t, r);
   ptx::st_release(slot, (uint64_t)nb);
   if ((uint32_t)seen != GAL_EMPTY_BLOCK) detach_block(st, (uint32_t)seen);
-  return nb;
+  *out = nb;
+  return REPLACE_OK;
 }
 
 // ---- slice tier ----------------------------------------------------------
 
-// Warp-aggregated slice allocation. Lanes asking for the same (tree, count)
-// form one group; its leader reserves the group's total with one atomic on
-// the pinned block's meta word and claims bits with fetch-and.
-__device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t c, uint64_t tid) {
+// Lanes of the tile of `width` lanes (8, 16 or 32) that holds this lane.
+__device__ __forceinline__ uint32_t tile_mask(uint32_t width) {
+  if (width >= 32) return 0xffffffffu;
+  const uint32_t lane = ptx::laneid();
+  return ((1u << width) - 1) << (lane & ~(width - 1));
+}
+
+// Warp-aggregated slice allocation of one run of 2^r slices of tree t. Lanes
+// asking for the same class form one group; its leader reserves the group's
+// total with one atomic on the pinned block's meta word and claims bits with
+// fetch-and. A group that finds every slot of its class full while the arena
+// has no block to replace them gives up (nullptr) instead of retrying.
+__device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t r, uint64_t tid,
+                                     uint32_t width = 32) {
+  const uint32_t c = 1u << r;
+  const uint32_t k = t + r;
   const uint32_t active = __activemask();
-  const uint32_t key = (t << 8) | (uint32_t)(__ffs((int)c) - 1);
-  const uint32_t peers = __match_any_sync(active, key);
+  const uint32_t peers = __match_any_sync(active, k) & tile_mask(width);
   const uint32_t lane = ptx::laneid();
   const uint32_t lt = ptx::lanemask_lt();
-  const uint32_t nslots = st->slot_count[t];
+  const uint32_t nslots = st->slot_count[k];
   const uint32_t slot0 = ptx::smid() % nslots;
-  uint64_t *const slots = st->slots + st->slot_offset[t];
-  const uint32_t ext_tree = (uint32_t)st->num_trees - 1;
+  uint64_t *const slots = st->slots + st->slot_offset[k];
   void *result = nullptr;
   bool done = false;
+  uint32_t strikes = 0;  // slots found full with no block to replace them
   for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
     const uint32_t grp = __ballot_sync(peers, !done);
     if (grp == 0) break;
@@ -469,11 +531,12 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
     const uint32_t g_n = __popc(grp);
     const uint32_t g_rank = __popc(grp & lt);
     const uint32_t need = g_n * c;
-    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3)) % nslots;
+    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3) + strikes) % nslots;
 
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
     uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
+    uint32_t nomem = 0;
     bool refill = false;
     if (lane == (uint32_t)leader) {
       const uint64_t sv = ptx::ld_acquire(slot);
@@ -482,7 +545,7 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
       if (b == GAL_EMPTY_BLOCK) {
         if (!replacing) {
           count(st, GAL_CTR_REPLACE_EMPTY);
-          b = replace_slot(st, slot, sv, t, tid);
+          nomem = replace_slot(st, slot, sv, t, r, tid, ADOPT_ANY, &b) == REPLACE_NOMEM;
         } else {
           count(st, GAL_CTR_SLOT_BUSY);
           backoff(attempt);
@@ -492,7 +555,7 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
         // the block stays usable while another leader replaces it
         uint64_t m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)need << GAL_META_CURSOR_SHIFT) | need);
         take = g_n;
-        if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED) {
+        if (meta_tree(m) != t || meta_run(m) != r || meta_state(m) != GAL_STATE_PINNED) {
           release_live(st, b, need);
           count(st, GAL_CTR_STALE_SLOT);
           take = 0;
@@ -504,7 +567,7 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
           if (take > 0) {
             const uint32_t part = take * c;
             m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)part << GAL_META_CURSOR_SHIFT) | part);
-            if (meta_tree(m) != t || meta_state(m) != GAL_STATE_PINNED ||
+            if (meta_tree(m) != t || meta_run(m) != r || meta_state(m) != GAL_STATE_PINNED ||
                 meta_live(m) + part > GAL_BLOCK_SLICES) {
               release_live(st, b, part);
               take = 0;
@@ -513,14 +576,15 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
           if (take == 0) {
             if (!replacing) {
               count(st, GAL_CTR_REPLACE_FULL);
-              replace_slot(st, slot, (uint64_t)b, t, tid);
+              uint32_t nb;
+              nomem = replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ANY, &nb) == REPLACE_NOMEM;
             } else {
               count(st, GAL_CTR_SLOT_BUSY);
               backoff(attempt);
             }
           }
         } else if (!replacing && meta_live(m) + need > kRefillMark) {
-          refill = true;  // swap in a fresh block once this group is served
+          refill = true;  // swap in another block once this group is served
         }
         if (take > 0) {
           cursor = meta_cursor(m) & (GAL_BLOCK_SLICES - 1);
@@ -528,6 +592,12 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
           b = GAL_EMPTY_BLOCK;
         }
       }
+      if (nomem) count(st, GAL_CTR_NOMEM);
+    }
+    nomem = __shfl_sync(grp, nomem, leader);
+    if (nomem && ++strikes >= nslots) {
+      done = true;  // every slot tried: the arena cannot serve this class now
+      continue;
     }
     b = __shfl_sync(grp, b, leader);
     if (b == GAL_EMPTY_BLOCK) continue;
@@ -548,11 +618,8 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
         if (pick) {
           const uint64_t mask = expand_runs(pick, c);
           const uint64_t old = ptx::atom_and_acquire(bits + w, ~mask);
-          const uint64_t gotbits = old & mask;
-          got = run_starts(gotbits, c) & pick;
-          const uint64_t partial = gotbits & ~expand_runs(got, c);
-          if (partial) ptx::red_or_relaxed(bits + w, partial);
-          if (c > 1 && got) ptx::red_or_relaxed(ext_words(st, b) + w, expand_runs(got, c) & ~got);
+          // a block serves one run length, so runs are taken or free whole
+          got = run_starts(old & mask, c) & pick;
           avail = old & ~mask;
         } else {
           avail = 0;
@@ -564,19 +631,13 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
       }
       got = ptx::shfl64(grp, got, leader);
       gw = __shfl_sync(grp, gw, leader);
-      const uint32_t k = (uint32_t)__popcll(got);
-      if (g_rank >= acc && g_rank < acc + k) my_slice = (int)(gw * 64 + (uint32_t)ptx::nth_set_bit(got, (int)(g_rank - acc)));
-      acc += k;
+      const uint32_t kk = (uint32_t)__popcll(got);
+      if (g_rank >= acc && g_rank < acc + kk) my_slice = (int)(gw * 64 + (uint32_t)ptx::nth_set_bit(got, (int)(g_rank - acc)));
+      acc += kk;
     }
     if (acc < take && lane == (uint32_t)leader) {
       release_live(st, b, (take - acc) * c);
       count(st, GAL_CTR_CLAIM_SHORT);
-      // a reservation that found no aligned run: the block is too fragmented
-      // for this run length, so give the slot a fresh block
-      if (c > 1) {
-        count(st, GAL_CTR_REPLACE_FRAG);
-        replace_slot(st, slot, (uint64_t)b, t, tid);
-      }
     }
     if (my_slice >= 0) {
       result = block_address(st, b, t) + ((uint64_t)my_slice << (st->min_shift + (int)t));
@@ -584,43 +645,36 @@ __device__ inline void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t
     }
     if (refill && lane == (uint32_t)leader) {
       count(st, GAL_CTR_REPLACE_REFILL);
-      replace_slot(st, slot, (uint64_t)b, t, tid, false);  // fresh blocks only
+      uint32_t nb;
+      replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ROOMY, &nb);  // no nearly-full blocks
     }
   }
-  if (!done) count(st, GAL_CTR_OOM_SLICE);
-  (void)ext_tree;
+  if (result == nullptr) count(st, GAL_CTR_OOM_SLICE);
   return result;
 }
 
 // Warp-aggregated slice free: one fetch-or per (block, word) and one
 // release of the live count per block.
-__device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t t, uint64_t off_s) {
-  const uint32_t active = __activemask();
+__device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t t, uint64_t off_s,
+                                  uint32_t width = 32) {
+  const uint32_t active = __activemask() & tile_mask(width);
   const int bis = block_index_shift(st);
   const uint64_t i = off_s >> (st->block_shift_min + (int)t);
   const uint64_t b = (seg << bis) + i;
   const uint32_t slice = (uint32_t)(off_s >> (st->min_shift + (int)t)) & (GAL_BLOCK_SLICES - 1);
   const uint32_t word = slice >> 6;
   const uint32_t bit = slice & 63;
+  // a block of the largest tree serves one run length, kept in its meta word
+  // (stable while this allocation holds the block out of its segment)
   uint32_t c = 1;
-  uint64_t *extw = nullptr;
-  if (t == (uint32_t)st->num_trees - 1) {
-    extw = ext_words(st, b) + word;
-    const uint64_t e = ptx::ld_relaxed(extw);
-    if (bit < 63) c = (uint32_t)__ffsll((long long)~(e >> (bit + 1)));
-  }
+  if (t == (uint32_t)st->num_trees - 1) c = 1u << meta_run(ptx::ld_relaxed(st->block_meta + b));
   const uint64_t mask = ((c >= 64) ? ~0ull : ((1ull << c) - 1)) << bit;
-  const uint64_t cont = mask & ~(1ull << bit);
   const uint32_t lane = ptx::laneid();
 
   const uint32_t wpeers = __match_any_sync(active, (unsigned long long)((b << 6) | word));
   const uint64_t or_mask = ptx::reduce_or64(wpeers, mask);
-  const uint64_t ext_mask = ptx::reduce_or64(wpeers, cont);
   __syncwarp(active);  // every lane's payload writes before the release below
-  if (lane == (uint32_t)(__ffs((int)wpeers) - 1)) {
-    if (ext_mask) ptx::red_and_relaxed(extw, ~ext_mask);
-    ptx::red_or_release(st->block_bits + (b << 6) + word, or_mask);
-  }
+  if (lane == (uint32_t)(__ffs((int)wpeers) - 1)) ptx::red_or_release(st->block_bits + (b << 6) + word, or_mask);
   const uint32_t bpeers = __match_any_sync(active, (unsigned long long)b);
   const uint32_t total = __reduce_add_sync(bpeers, c);
   __syncwarp(active);  // bitmap returns before the live count drops
@@ -631,12 +685,12 @@ __device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t 
 
 __device__ inline void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_t tid) {
   bool adopted = false;
-  const uint32_t b = request_block(st, bt, tid, false, &adopted);
+  const uint32_t b = request_block(st, bt, 0, 1, tid, ADOPT_NONE, &adopted);
   if (b == GAL_EMPTY_BLOCK) {
     count(st, GAL_CTR_OOM_BLOCK);
     return nullptr;
   }
-  own_block(st, b, bt, GAL_STATE_DETACHED, 1);
+  own_block(st, b, bt, 0, GAL_STATE_WHOLE, 1);
   return block_address(st, b, bt);
 }
 
@@ -682,15 +736,17 @@ __device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_
 
 // ---- public entry points -------------------------------------------------
 
-__device__ inline void *malloc(const gal_state_t *st, uint64_t size) {
+// `width` limits warp aggregation to tiles of 8, 16 or 32 lanes (the
+// reference groups the whole coalesced warp, gallatin.cuh:883-885).
+__device__ inline void *malloc(const gal_state_t *st, uint64_t size, uint32_t width = 32) {
   const size_class sc = classify(st, size);
   const uint64_t tid = veb::thread_tid();
-  if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, sc.count, tid);
+  if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, (uint32_t)(__ffs((int)sc.count) - 1), tid, width);
   if (sc.tier == TIER_BLOCK) return malloc_block(st, sc.tree, tid);
   return malloc_segment(st, sc.nseg);
 }
 
-__device__ inline void free(const gal_state_t *st, void *ptr) {
+__device__ inline void free(const gal_state_t *st, void *ptr, uint32_t width = 32) {
   if (ptr == nullptr) return;
   const uint64_t off = (uint64_t)((char *)ptr - st->memory);
   if (off >= st->arena_bytes) {
@@ -700,7 +756,7 @@ __device__ inline void free(const gal_state_t *st, void *ptr) {
   const uint64_t seg = off >> st->segment_shift;
   const uint16_t id = ptx::ld_relaxed(st->chunk_ids + seg);
   if (id < (uint16_t)st->num_trees) {
-    free_slice(st, seg, id, off & (st->segment_bytes - 1));
+    free_slice(st, seg, id, off & (st->segment_bytes - 1), width);
   } else if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees) {
     free_segment(st, seg, id);
   } else {

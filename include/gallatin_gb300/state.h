@@ -16,12 +16,17 @@
  *   seg_block_bits  u64[num_segments * seg_block_words]  1 = block free
  *   block_meta      u64[num_segments * blocks_per_segment]  see GAL_META_*
  *   block_bits      u64[num_segments * blocks_per_segment * 64]  1 = slice free
- *   block_ext       u64[num_segments * ext_blocks_per_segment * 64] marks the
- *                   continuation slices of multi-slice runs (largest tree only)
- *   slots           u64[total_slots]    pinned block per (tree, SM slot)
+ *   slots           u64[total_slots]    pinned block per (slot class, SM slot)
  *   veb bit layers  one u64 array per layer per tree: the segment tree and
- *                   the per-tree sub trees over segment ids, and the per-tree
- *                   adoptable-block trees over block ids
+ *                   the per-tree sub trees over segment ids, and per slot
+ *                   class two trees over block ids (detached blocks with room,
+ *                   and the subset that drained to half a block or less)
+ *
+ * Slot classes: class t < num_trees-1 serves single slices of tree t; the
+ * largest tree has one class per run length 2^r (r = 0 .. num_classes -
+ * num_trees), class num_trees-1+r. A block of the largest tree serves one
+ * run length for as long as it is out of its segment, so its free slices
+ * always form aligned runs of that length.
  */
 #ifndef GALLATIN_GB300_STATE_H
 #define GALLATIN_GB300_STATE_H
@@ -42,17 +47,23 @@
  *   bits  0-31  live: slices reserved or held (reservations precede claims)
  *   bits 32-39  tree id the block is formatted for
  *   bits 40-41  state: FREE (in its segment's pool), PINNED (serving a slot),
- *               DETACHED (no longer pinned; recycled when live reaches 0)
+ *               DETACHED (no longer pinned; recycled when live reaches 0),
+ *               WHOLE (one block-tier allocation)
+ *   bits 42-45  log2 of the run length the block serves (largest tree only)
  *   bits 48-63  cursor: position hint for the next claim, wraps mod 2^16
  * All transitions are atomic adds of field deltas (or a CAS for the
  * conditional retire) so concurrent reservations and their undos commute. */
 #define GAL_META_LIVE_MASK 0xFFFFFFFFull
 #define GAL_META_TREE_SHIFT 32
 #define GAL_META_STATE_SHIFT 40
+#define GAL_META_RUN_SHIFT 42
 #define GAL_META_CURSOR_SHIFT 48
 #define GAL_STATE_FREE 0u
 #define GAL_STATE_PINNED 1u
 #define GAL_STATE_DETACHED 2u
+#define GAL_STATE_WHOLE 3u
+/* a detached block is listed for early reuse once live <= this */
+#define GAL_ROOMY_MARK (GAL_BLOCK_SLICES / 2)
 
 /* slot word: low 32 bits block id (GAL_EMPTY_BLOCK when none), bit 32 set
  * while one leader is replacing the block. */
@@ -77,7 +88,9 @@ enum gal_counter_id {
   GAL_CTR_STALE_SLOT = 14,    /* slot changed between read and reservation */
   GAL_CTR_SLOT_BUSY = 15,     /* slot was being replaced */
   GAL_CTR_REPLACE_REFILL = 16, /* pinned block replaced ahead of filling up */
-  GAL_CTR_ADOPT = 17,          /* detached block with room pinned again */
+  GAL_CTR_ADOPT = 17,          /* detached block with room pinned again (arena full) */
+  GAL_CTR_ADOPT_ROOMY = 18,    /* detached block at or under half live pinned again */
+  GAL_CTR_NOMEM = 19,          /* slot found full with no block to replace it */
   GAL_CTR_TREE_PINS = 32,     /* + tree id: blocks pinned per tree */
   GAL_NUM_COUNTERS = 64
 };
@@ -104,7 +117,7 @@ typedef struct gal_state_t {
   int32_t block_shift_min;  /* log2(smallest slice * 4096) */
   uint32_t blocks_per_segment;     /* for tree 0; tree t has this >> t */
   uint32_t seg_block_words;        /* u64 words per segment block bitmap */
-  uint32_t ext_blocks_per_segment; /* blocks_per_segment >> (num_trees-1) */
+  uint32_t num_classes;            /* slot classes, see above */
   uint32_t num_sms;
   uint32_t total_slots;
   uint32_t slot_count[GAL_MAX_TREES];
@@ -117,16 +130,18 @@ typedef struct gal_state_t {
   uint64_t *seg_block_bits;
   uint64_t *block_meta;
   uint64_t *block_bits;
-  uint64_t *block_ext;
   uint64_t *slots;
   uint32_t *locks;                 /* bit t: tree t attach lock; bit 31: segment tier */
   unsigned long long *counters;    /* GAL_NUM_COUNTERS */
 
   gal_veb_t segment_tree;
   gal_veb_t sub_trees[GAL_MAX_TREES];
-  /* per tree: DETACHED blocks (universe = all block ids) that a slot can pin
-   * again when no fresh block is left, so their free slices stay reachable */
+  /* per slot class: DETACHED blocks (universe = all block ids) that a slot
+   * can pin again when no fresh block is left, so their free slices stay
+   * reachable; roomy_trees lists those with live <= GAL_ROOMY_MARK, which
+   * are pinned again before a fresh block is taken */
   gal_veb_t adopt_trees[GAL_MAX_TREES];
+  gal_veb_t roomy_trees[GAL_MAX_TREES];
 } gal_state_t;
 
 #endif /* GALLATIN_GB300_STATE_H */

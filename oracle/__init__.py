@@ -85,6 +85,8 @@ def load_replay():
         ]
         lib.cpu_replay_pairs.restype = c_double
         lib.cpu_replay_pairs.argtypes = [c_uint64, c_uint64, c_int, POINTER(c_uint64), POINTER(c_uint64)]
+        lib.cpu_replay_batches.restype = c_double
+        lib.cpu_replay_batches.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_int, POINTER(c_uint64)]
         lib.cpu_mixed_classes.restype = None
         lib.cpu_mixed_classes.argtypes = [c_uint64, c_uint32, c_uint64, c_void_p]
         _REPLAY = lib
@@ -104,6 +106,17 @@ def cpu_replay_mixed(n, tid_begin, tid_end, rounds, seed, *, seg_every=0, block_
     secs = load_replay().cpu_replay_mixed(n, tid_begin, tid_end, rounds, seed, ptr, seg_every, block_dim, seg_lo,
                                           seg_hi, workers, ctypes.byref(misses), ctypes.byref(bad))
     return secs, misses.value, bad.value
+
+
+def cpu_replay_batches(reqs: np.ndarray, offsets: np.ndarray, table_slots: int, workers: int = 1):
+    """glibc malloc/free over the batched request stream; returns (seconds, misses)."""
+    reqs = np.ascontiguousarray(reqs, dtype=np.uint64)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    table = np.zeros(table_slots + 1, dtype=np.uint64)
+    misses = c_uint64(0)
+    secs = load_replay().cpu_replay_batches(reqs.ctypes.data, offsets.ctypes.data, len(offsets) - 1,
+                                            table.ctypes.data, workers, ctypes.byref(misses))
+    return secs, misses.value
 
 
 def cpu_replay_pairs(n, size, workers=1):
@@ -149,6 +162,7 @@ def _bind_ref(lib):
         "galref_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
         "galref_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "galref_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "galref_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -218,6 +232,12 @@ class RefGallatin:
                                            block_dim, out.ctypes.data, stream) != 0:
             raise RuntimeError("galref_run_mixed_host failed")
         return out
+
+    def run_batches(self, d_reqs, d_offsets, offsets, d_table, d_stats, *, persistent=False, stream=0):
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        if self._lib.galref_run_batches(self._h, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1, d_table,
+                                        1 if persistent else 0, d_stats, stream) != 0:
+            raise RuntimeError("galref_run_batches failed")
 
     def close(self):
         if self._h:

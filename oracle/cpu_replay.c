@@ -171,3 +171,60 @@ void cpu_mixed_classes(uint64_t n, uint32_t rounds, uint64_t seed, uint8_t *out)
     for (uint32_t r = 0; r < rounds; ++r) out[(uint64_t)r * n + tid] = (uint8_t)(xorshift64(&s) % 9);
   }
 }
+
+/* Batched request stream (slot << 32 | size; size 0 = free): the requests of
+ * a batch are split over the workers, batches run one after another. */
+typedef struct {
+  const uint64_t *reqs;
+  uint64_t begin, end;
+  uint64_t *table;
+  uint64_t misses;
+} batch_job;
+
+static void *run_batch_part(void *arg) {
+  batch_job *j = (batch_job *)arg;
+  uint64_t misses = 0;
+  for (uint64_t i = j->begin; i < j->end; ++i) {
+    const uint64_t r = j->reqs[i];
+    const uint32_t slot = (uint32_t)(r >> 32);
+    const uint32_t size = (uint32_t)r;
+    if (size) {
+      void *p = malloc(size);
+      if (!p) misses++;
+      j->table[slot] = (uint64_t)p;
+    } else {
+      free((void *)j->table[slot]);
+      j->table[slot] = 0;
+    }
+  }
+  j->misses = misses;
+  return NULL;
+}
+
+double cpu_replay_batches(const uint64_t *reqs, const uint64_t *offsets, uint32_t n_batches, uint64_t *table,
+                          int workers, uint64_t *misses) {
+  if (workers < 1) workers = 1;
+  if (workers > 1024) workers = 1024;
+  batch_job *jobs = (batch_job *)calloc((size_t)workers, sizeof(batch_job));
+  pthread_t *th = (pthread_t *)calloc((size_t)workers, sizeof(pthread_t));
+  *misses = 0;
+  double t0 = now_s();
+  for (uint32_t b = 0; b < n_batches; ++b) {
+    const uint64_t lo = offsets[b], n = offsets[b + 1] - offsets[b];
+    for (int w = 0; w < workers; ++w) {
+      jobs[w].reqs = reqs;
+      jobs[w].table = table;
+      jobs[w].begin = lo + n * (uint64_t)w / (uint64_t)workers;
+      jobs[w].end = lo + n * (uint64_t)(w + 1) / (uint64_t)workers;
+      pthread_create(&th[w], NULL, run_batch_part, &jobs[w]);
+    }
+    for (int w = 0; w < workers; ++w) {
+      pthread_join(th[w], NULL);
+      *misses += jobs[w].misses;
+    }
+  }
+  double t1 = now_s();
+  free(jobs);
+  free(th);
+  return t1 - t0;
+}

@@ -99,9 +99,56 @@ int launch_mixed(void *dev, uint64_t n, uint32_t rounds, uint64_t seed, uint32_t
   return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
+template <class G>
+int launch_batches(void *dev, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
+                   uint32_t n_batches, uint64_t *d_table, uint32_t mode, unsigned long long *stats, cudaStream_t s) {
+  G *a = (G *)dev;
+  if (mode == 0) {
+    for (uint32_t b = 0; b < n_batches; ++b) {
+      const uint64_t n = h_offsets[b + 1] - h_offsets[b];
+      if (n == 0) continue;
+      galwork::batch_kernel<G><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, d_reqs + h_offsets[b], n, d_table, 32,
+                                                                           stats);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+  }
+  int per_sm = 0, dev_id = 0;
+  cudaDeviceProp prop;
+  cudaGetDevice(&dev_id);
+  cudaGetDeviceProperties(&prop, dev_id);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, galwork::persistent_batches_kernel<G>, 256, 0);
+  if (per_sm < 1) return 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(per_sm * prop.multiProcessorCount);
+  cfg.blockDim = dim3(256);
+  cfg.stream = s;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeCooperative;
+  attr.val.cooperative = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  uint32_t width = 32;
+  return cudaLaunchKernelEx(&cfg, galwork::persistent_batches_kernel<G>, a, d_reqs, d_offsets, n_batches, d_table,
+                            width, stats) == cudaSuccess ? 0 : 2;
+}
+
 }  // namespace
 
 extern "C" {
+
+int galref_run_batches(void *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
+                       uint32_t n_batches, uint64_t *d_table, uint32_t mode, unsigned long long *d_stats,
+                       void *stream) {
+  RefAlloc *a = (RefAlloc *)h;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a->config) {
+    case 0: return launch_batches<ref_16m_16_4096>(a->dev, d_reqs, d_offsets, h_offsets, n_batches, d_table, mode, d_stats, s);
+    case 1: return launch_batches<ref_16m_128_4096>(a->dev, d_reqs, d_offsets, h_offsets, n_batches, d_table, mode, d_stats, s);
+    case 2: return launch_batches<ref_64m_16_4096>(a->dev, d_reqs, d_offsets, h_offsets, n_batches, d_table, mode, d_stats, s);
+    default: return launch_batches<ref_4m_16_1024>(a->dev, d_reqs, d_offsets, h_offsets, n_batches, d_table, mode, d_stats, s);
+  }
+}
+
 
 int galref_veb_create(uint64_t universe, uint64_t seed, void **out) {
   RefTree *r = new RefTree();

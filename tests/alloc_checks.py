@@ -85,8 +85,10 @@ def check_restored(alloc: gal.Gallatin) -> None:
     for t in range(alloc.num_trees):
         for layer in alloc.veb_layers(t):
             assert not layer.any(), f"sub tree {t} not empty"
-        for layer in alloc.veb_layers(t, "adopt_tree"):
-            assert not layer.any(), f"adoptable-block tree {t} not empty"
+    for k in range(alloc.num_classes):
+        for kind in ("adopt_tree", "roomy_tree"):
+            for layer in alloc.veb_layers(k, kind):
+                assert not layer.any(), f"{kind} of slot class {k} not empty"
     ids = alloc.dump("chunk_ids")
     assert (ids == gal.GAL_FREE_SEGMENT).all(), "memory table not reset"
     avail = alloc.dump("seg_avail")
@@ -96,8 +98,6 @@ def check_restored(alloc: gal.Gallatin) -> None:
     live = meta & np.uint64(0xFFFFFFFF)
     assert (state == 0).all(), "blocks left outside their pools"
     assert (live == 0).all(), "live counts not balanced"
-    ext = alloc.dump("block_ext")
-    assert not ext.any(), "multi-slice continuation bits left set"
     slots = alloc.dump("slots")
     assert (slots == gal.GAL_EMPTY_BLOCK).all()
     assert int(alloc.dump("locks")[0]) == 0

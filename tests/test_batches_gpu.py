@@ -1,0 +1,126 @@
+"""Batched request streams: the persistent kernel, its CUDA graph and the plain
+per-batch path serve the same stream with the same outcome, and the allocator
+ends empty."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import gallatin_gb300 as gal
+from alloc_checks import check_live, check_restored
+
+pytestmark = pytest.mark.gpu
+
+
+def small_trace(seed=5):
+    from gallatin_gb300.workload import batch_trace
+
+    return batch_trace(seed, n_batches=12, batch_lo=1024, batch_hi=40000)
+
+
+@pytest.mark.parametrize("persistent,width", [(False, 32), (True, 32), (True, 16), (True, 8)])
+def test_batches_serve_stream_and_restore(cuda, persistent, width):
+    reqs, offsets, slots, info = small_trace()
+    with gal.Gallatin.generate_on_device(1 << 30, 3, print_info=False) as a:
+        d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        # all but the drain batch: the table then holds the live set
+        a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets[:-1], d_table.data_ptr(), stats.data_ptr(),
+                      width=width, persistent=persistent)
+        cuda.cuda.synchronize()
+        assert int(stats[0]) == 0
+        table = d_table.cpu().numpy().view(np.uint64)
+        # sizes of the live slots, from the host replay of the stream
+        sizes = np.zeros(slots + 1, dtype=np.uint64)
+        for r in reqs[: int(offsets[-2])]:
+            slot, size = int(r >> np.uint64(32)), int(r & np.uint64(0xFFFFFFFF))
+            sizes[slot] = size
+        live = table != 0
+        check_live(a, table[live], sizes[live])
+        # the drain batch frees the rest
+        drain = offsets[-2:]
+        d_drain = cuda.from_numpy((drain - drain[0]).view(np.int64)).cuda()
+        d_reqs_drain = cuda.from_numpy(reqs[int(drain[0]):].view(np.int64).copy()).cuda()
+        a.run_batches(d_reqs_drain.data_ptr(), d_drain.data_ptr(), drain - drain[0], d_table.data_ptr(),
+                      stats.data_ptr(), width=width, persistent=persistent)
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        assert not d_table.any()
+        check_restored(a)
+
+
+def test_graph_replay_repeats_the_stream(cuda):
+    reqs, offsets, slots, info = small_trace(7)
+    with gal.Gallatin.generate_on_device(1 << 30, 4, print_info=False) as a:
+        d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        with a.capture_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(),
+                               stats.data_ptr(), persistent=True) as g:
+            for _ in range(3):
+                g.launch()
+            cuda.cuda.synchronize()
+        assert int(stats[0]) == 0
+        assert not d_table.any()  # every replay ends with the drain batch
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        check_restored(a)
+
+
+def test_batches_host_entry_point(cuda):
+    reqs, offsets, slots, info = small_trace(9)
+    with gal.Gallatin.generate_on_device(1 << 30, 4, print_info=False) as a:
+        out = a.run_batches_host(reqs, offsets, slots, persistent=True)
+        assert out[0] == 0
+        out = a.run_batches_host(reqs, offsets, slots, persistent=False, width=16)
+        assert out[0] == 0
+
+
+def test_reference_plain_path_on_the_same_stream(cuda):
+    import oracle
+
+    if oracle.load_ref() is None:
+        pytest.skip("reference build not available on this box")
+    reqs, offsets, slots, info = small_trace(11)
+    assert info["max_request_bytes"] <= 16 << 20  # never the reference's segment tier
+    ref = oracle.RefGallatin(1 << 30, 4)
+    try:
+        d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        ref.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(), stats.data_ptr())
+        cuda.cuda.synchronize()
+        assert int(stats[0]) == 0
+        assert not d_table.any()
+    finally:
+        ref.close()
+
+
+@pytest.mark.parametrize("persistent", [False, True])
+def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent):
+    """Allocations live across many batches and are freed in random order, the
+    live set peaking at about half the arena in size-class bytes: no request
+    may fail, and the state restores after the drain."""
+    from gallatin_gb300.workload import batch_trace
+
+    reqs, offsets, slots, info = batch_trace(5, n_batches=40, batch_lo=1024, batch_hi=131072)
+    arena = 1280 << 20
+    assert info["peak_class_bytes"] <= arena // 2
+    with gal.Gallatin.generate_on_device(arena, 6, print_info=False) as a:
+        d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(), stats.data_ptr(),
+                      persistent=persistent)
+        cuda.cuda.synchronize()
+        c = a.stats()["counters"]
+        assert int(stats[0]) == 0, c
+        assert c["timeout"] == 0 and c["corrupt"] == 0, c
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        check_restored(a)
