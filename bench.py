@@ -47,7 +47,7 @@ WORKLOADS = {
     "pairs": dict(arena=2 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=1_048_576, size=16, block=1024),
     # the batching configuration: 64 batches of 1k-512k requests, lognormal
     # sizes, 60/40 malloc/free over the live set, plus a drain batch
-    "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32),
+    "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32, binned=True),
     # the mixed workload without its 256 segment-tier requests: only the
     # slice tier runs, which is what the reference arm can be compared on
     "mixed-slices": dict(
@@ -304,14 +304,14 @@ def run(args) -> dict | None:
 
             e2e_step = None
         else:
-            graph = a.capture_batches(*bargs, width=w["width"], persistent=True)
+            graph = a.capture_batches(*bargs, width=w["width"], persistent=True, binned=w["binned"])
 
             def step():
                 graph.launch(s_ptr)
 
             def e2e_step():
-                return a.run_batches_host(reqs, offsets, slots, width=w["width"], persistent=True, stream=s_ptr,
-                                          reqs_ptr=h_reqs.data_ptr())
+                return a.run_batches_host(reqs, offsets, slots, width=w["width"], persistent=True,
+                                          binned=w["binned"], stream=s_ptr, reqs_ptr=h_reqs.data_ptr())
 
         h2d = units * 8 + len(offsets) * 8
         config = {
@@ -321,7 +321,8 @@ def run(args) -> dict | None:
             "max_size": w["max_size"], "requests": units, "mallocs": info["mallocs"], "frees": info["frees"],
             "max_live": info["max_live"], "max_request_bytes": info["max_request_bytes"], "seed": 42,
             "path": ("reference: one launch per batch" if impl == "reference"
-                     else f"persistent cooperative kernel in a CUDA graph, aggregation width {w['width']}"),
+                     else f"persistent cooperative kernel in a CUDA graph, aggregation width {w['width']}"
+                          + (", each batch counting-sorted by size class on the device" if w["binned"] else "")),
             "l2": "flushed (256 MiB write) before every timed step",
         }
     else:

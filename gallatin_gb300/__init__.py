@@ -108,6 +108,14 @@ class GalError(RuntimeError):
     """A C-ABI call returned an error status."""
 
 
+def _batch_mode(persistent: bool, binned: bool) -> int:
+    if not persistent:
+        if binned:
+            raise ValueError("binned batches need the persistent path")
+        return 0
+    return 2 if binned else 1
+
+
 class _Geometry(ctypes.Structure):
     _fields_ = [
         ("segment_bytes", c_uint64),
@@ -179,11 +187,11 @@ def load(path: str | Path | None = None):
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host_noalloc": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
-        "gal_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, vp, vp]),
-        "gal_capture_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, vp, POINTER(vp)]),
+        "gal_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, u32, vp, vp]),
+        "gal_capture_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, u32, vp, POINTER(vp)]),
         "gal_graph_launch": (i32, [vp, vp]),
         "gal_graph_destroy": (i32, [vp]),
-        "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, vp, vp]),
+        "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, u32, vp, vp]),
         "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
         "gal_veb_destroy": (i32, [vp]),
         "gal_veb_num_layers": (i32, [vp]),
@@ -400,29 +408,35 @@ class Gallatin:
 
     # -- batched request streams ---------------------------------------------
     def run_batches(self, d_reqs: int, d_offsets: int, offsets: np.ndarray, d_table: int, d_stats: int, *,
-                    width: int = 32, persistent: bool = True, stream: int = 0) -> None:
+                    width: int = 32, persistent: bool = True, binned: bool = False, ctas_per_sm: int = 0,
+                    stream: int = 0) -> None:
         """Serve a batched request stream (see gal_run_batches); `offsets` is
-        the host copy of the batch offsets."""
+        the host copy of the batch offsets. persistent=False is the plain
+        one-launch-per-batch path; binned sorts each batch by size class;
+        ctas_per_sm sets the persistent grid (0 = as many as fit)."""
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         _check(load().gal_run_batches(self.handle, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1, d_table,
-                                      width, 1 if persistent else 0, d_stats, stream))
+                                      width, _batch_mode(persistent, binned), ctas_per_sm, d_stats, stream))
 
     def capture_batches(self, d_reqs: int, d_offsets: int, offsets: np.ndarray, d_table: int, d_stats: int, *,
-                        width: int = 32, persistent: bool = True) -> "Graph":
+                        width: int = 32, persistent: bool = True, binned: bool = False,
+                        ctas_per_sm: int = 0) -> "Graph":
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         g = c_void_p()
         _check(load().gal_capture_batches(self.handle, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1,
-                                          d_table, width, 1 if persistent else 0, d_stats, ctypes.byref(g)))
+                                          d_table, width, _batch_mode(persistent, binned), ctas_per_sm, d_stats,
+                                          ctypes.byref(g)))
         return Graph(g.value)
 
     def run_batches_host(self, reqs: np.ndarray, offsets: np.ndarray, table_slots: int, *, width: int = 32,
-                         persistent: bool = True, stream: int = 0, reqs_ptr: int | None = None) -> np.ndarray:
+                         persistent: bool = True, binned: bool = False, ctas_per_sm: int = 0, stream: int = 0,
+                         reqs_ptr: int | None = None) -> np.ndarray:
         """End to end from host buffers; returns the 8 stats words."""
         offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
         out = np.zeros(8, dtype=np.uint64)
         ptr = reqs_ptr if reqs_ptr is not None else np.ascontiguousarray(reqs, dtype=np.uint64).ctypes.data
         _check(load().gal_run_batches_host(self.handle, ptr, offsets.ctypes.data, len(offsets) - 1, table_slots, width,
-                                           1 if persistent else 0, out.ctypes.data, stream))
+                                           _batch_mode(persistent, binned), ctas_per_sm, out.ctypes.data, stream))
         return out
 
     # -- inspection -----------------------------------------------------------

@@ -1,6 +1,7 @@
 // C ABI: batched request streams (the batching configuration): one launch per
-// batch, or one cooperative persistent launch over all batches, optionally
-// captured once into a CUDA graph and replayed.
+// batch, or one cooperative persistent launch over all batches (as given, or
+// with every batch counting-sorted by size class first), optionally captured
+// once into a CUDA graph and replayed.
 #include <cuda_runtime.h>
 
 #include "capi_internal.h"
@@ -11,9 +12,48 @@ namespace {
 
 constexpr unsigned kBatchBlock = 256;
 
+int grow(void **p, uint64_t *have, uint64_t need, const char *what) {
+  if (need <= *have) return GAL_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  GAL_CUDA_TRY(cudaMalloc(p, need), what);
+  *have = need;
+  return GAL_OK;
+}
+
+// Scratch of the binned path, sized for the largest batch. Grown before a
+// launch or a capture, never inside one.
+int ensure_bin_scratch(gal_allocator *h, const uint64_t *h_offsets, uint32_t n_batches) {
+  uint64_t most = 0;
+  for (uint32_t b = 0; b < n_batches; ++b) {
+    const uint64_t n = h_offsets[b + 1] - h_offsets[b];
+    if (n > most) most = n;
+  }
+  if (most > 0xFFFFFFFFull) return galcapi::fail_invalid("a batch of the binned path holds at most 2^32-1 requests");
+  int rc = grow((void **)&h->d_bsorted, &h->d_bsorted_bytes, most * 8 + 8, "cudaMalloc sorted batch");
+  if (rc != GAL_OK) return rc;
+  return grow((void **)&h->d_bbins, &h->d_bbins_bytes, 4ull * galwork::kBins * 4, "cudaMalloc batch bins");
+}
+
+// ctas_per_sm: kernel geometry, 0 = as many as fit (every CTA must be
+// resident for the grid barrier, so more than fit is refused)
+template <class K>
+int launch_cooperative(gal_allocator *h, K kernel, uint32_t ctas_per_sm, cudaStream_t s, void **args) {
+  int per_sm = 0;
+  GAL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBatchBlock, 0), "occupancy query");
+  if (per_sm < 1) return galcapi::fail_invalid("persistent batch kernel does not fit on an SM");
+  if (ctas_per_sm > (uint32_t)per_sm) return galcapi::fail_invalid("more CTAs per SM than fit");
+  if (ctas_per_sm) per_sm = (int)ctas_per_sm;
+  GAL_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)kernel, dim3(per_sm * h->hs.num_sms), dim3(kBatchBlock),
+                                           args, 0, s),
+               "persistent batch launch");
+  return GAL_OK;
+}
+
 int launch_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
-                   uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode, unsigned long long *d_stats,
-                   cudaStream_t s) {
+                   uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
+                   unsigned long long *d_stats, cudaStream_t s) {
   gal_device_alloc *a = reinterpret_cast<gal_device_alloc *>(h->d_state);
   if (mode == 0) {
     for (uint32_t b = 0; b < n_batches; ++b) {
@@ -25,59 +65,58 @@ int launch_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_o
     GAL_CUDA_TRY(cudaGetLastError(), "batch launch");
     return GAL_OK;
   }
-  int per_sm = 0;
-  GAL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, galwork::persistent_batches_kernel<gal_device_alloc>, kBatchBlock, 0),
-               "occupancy query");
-  if (per_sm < 1) return galcapi::fail_invalid("persistent batch kernel does not fit on an SM");
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(per_sm * h->hs.num_sms);
-  cfg.blockDim = dim3(kBatchBlock);
-  cfg.stream = s;
-  cudaLaunchAttribute attr;
-  attr.id = cudaLaunchAttributeCooperative;
-  attr.val.cooperative = 1;
-  cfg.attrs = &attr;
-  cfg.numAttrs = 1;
-  GAL_CUDA_TRY(cudaLaunchKernelEx(&cfg, galwork::persistent_batches_kernel<gal_device_alloc>, a, d_reqs, d_offsets,
-                                  n_batches, d_table, width, d_stats),
-               "persistent batch launch");
-  return GAL_OK;
+  if (mode == 1) {
+    void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats};
+    return launch_cooperative(h, galwork::persistent_batches_kernel<gal_device_alloc>, ctas_per_sm, s, args);
+  }
+  int rc = ensure_bin_scratch(h, h_offsets, n_batches);
+  if (rc != GAL_OK) return rc;
+  GAL_CUDA_TRY(cudaMemsetAsync(h->d_bbins, 0, 4ull * galwork::kBins * 4, s), "bins reset");
+  uint64_t *sorted = h->d_bsorted;
+  uint32_t *bins = h->d_bbins;
+  void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats, &sorted, &bins};
+  return launch_cooperative(h, galwork::binned_batches_kernel<gal_device_alloc>, ctas_per_sm, s, args);
 }
 
 bool valid_width(uint32_t w) { return w == 8 || w == 16 || w == 32; }
+constexpr const char *kModeError = "mode must be 0 (per batch), 1 (persistent) or 2 (persistent, binned)";
 
 }  // namespace
 
 extern "C" int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets,
                                const uint64_t *h_offsets, uint32_t n_batches, uint64_t *d_table, uint32_t width,
-                               uint32_t mode, unsigned long long *d_stats, void *stream) {
+                               uint32_t mode, uint32_t ctas_per_sm, unsigned long long *d_stats, void *stream) {
   if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
       d_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
   if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
-  if (mode > 1) return galcapi::fail_invalid("mode must be 0 (per batch) or 1 (persistent)");
-  return launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, d_stats,
+  if (mode > 2) return galcapi::fail_invalid(kModeError);
+  return launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, ctas_per_sm, d_stats,
                         (cudaStream_t)stream);
 }
 
 extern "C" int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets,
                                    const uint64_t *h_offsets, uint32_t n_batches, uint64_t *d_table, uint32_t width,
-                                   uint32_t mode, unsigned long long *d_stats, void **graph_out) {
+                                   uint32_t mode, uint32_t ctas_per_sm, unsigned long long *d_stats,
+                                   void **graph_out) {
   if (graph_out == nullptr) return galcapi::fail_invalid("graph_out is NULL");
   *graph_out = nullptr;
   if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
       d_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
   if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
-  if (mode > 1) return galcapi::fail_invalid("mode must be 0 (per batch) or 1 (persistent)");
+  if (mode > 2) return galcapi::fail_invalid(kModeError);
+  if (mode == 2) {
+    const int rc = ensure_bin_scratch(h, h_offsets, n_batches);  // no allocation inside the capture
+    if (rc != GAL_OK) return rc;
+  }
   cudaStream_t s;
   GAL_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "capture stream");
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
   int rc = GAL_OK;
   if (e == cudaSuccess) {
-    rc = launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, d_stats, s);
+    rc = launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, ctas_per_sm, d_stats, s);
     cudaError_t e2 = cudaStreamEndCapture(s, &graph);
     if (rc == GAL_OK && e2 != cudaSuccess) rc = galcapi::fail_cuda(e2, "end capture");
   } else {
@@ -106,21 +145,9 @@ extern "C" int gal_graph_destroy(void *graph_exec) {
   return GAL_OK;
 }
 
-namespace {
-int grow(void **p, uint64_t *have, uint64_t need, const char *what) {
-  if (need <= *have) return GAL_OK;
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-  *have = 0;
-  GAL_CUDA_TRY(cudaMalloc(p, need), what);
-  *have = need;
-  return GAL_OK;
-}
-}  // namespace
-
 extern "C" int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_t *h_offsets,
                                     uint32_t n_batches, uint64_t table_slots, uint32_t width, uint32_t mode,
-                                    uint64_t *h_stats, void *stream) {
+                                    uint32_t ctas_per_sm, uint64_t *h_stats, void *stream) {
   if (h == nullptr || h_reqs == nullptr || h_offsets == nullptr || h_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
   const uint64_t nreq = h_offsets[n_batches];
@@ -134,7 +161,8 @@ extern "C" int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, co
   GAL_CUDA_TRY(cudaMemcpyAsync(h->d_breqs, h_reqs, nreq * 8, cudaMemcpyHostToDevice, s), "requests H2D");
   GAL_CUDA_TRY(cudaMemcpyAsync(h->d_boffs, h_offsets, (n_batches + 1) * 8ull, cudaMemcpyHostToDevice, s),
                "offsets H2D");
-  rc = gal_run_batches(h, h->d_breqs, h->d_boffs, h_offsets, n_batches, h->d_btable, width, mode, h->d_stats, stream);
+  rc = gal_run_batches(h, h->d_breqs, h->d_boffs, h_offsets, n_batches, h->d_btable, width, mode, ctas_per_sm,
+                       h->d_stats, stream);
   if (rc != GAL_OK) return rc;
   GAL_CUDA_TRY(cudaMemcpyAsync(h_stats, h->d_stats, 64, cudaMemcpyDeviceToHost, s), "stats D2H");
   GAL_CUDA_TRY(cudaStreamSynchronize(s), "batch e2e sync");

@@ -111,6 +111,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   const int max_shift = log2_exact(max_size);
   const int num_trees = max_shift - min_shift + 1;
   if (num_trees > GAL_MAX_TREES) return fail_invalid("too many size classes");
+  if (num_segments * (segment_bytes / (min_size * 4096)) >= 0xFFFFFFF0ull)
+    return fail_invalid("too many blocks: block ids are 32-bit");
   if ((uint64_t)num_trees + 2 + 1 > 0xFFFEull) return fail_invalid("too many size classes");
 
   int dev = 0;
@@ -125,6 +127,9 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   h->d_stats = nullptr;
   h->d_breqs = h->d_boffs = h->d_btable = nullptr;
   h->d_breqs_bytes = h->d_boffs_bytes = h->d_btable_bytes = 0;
+  h->d_bsorted = nullptr;
+  h->d_bbins = nullptr;
+  h->d_bsorted_bytes = h->d_bbins_bytes = 0;
   h->min_size = min_size;
   h->max_size = max_size;
   gal_state_t &s = h->hs;
@@ -244,6 +249,8 @@ extern "C" int gal_destroy(gal_allocator *h) {
   if (h->d_breqs) cudaFree(h->d_breqs);
   if (h->d_boffs) cudaFree(h->d_boffs);
   if (h->d_btable) cudaFree(h->d_btable);
+  if (h->d_bsorted) cudaFree(h->d_bsorted);
+  if (h->d_bbins) cudaFree(h->d_bbins);
   free_all(h->device_allocs);
   delete h;
   if (e != cudaSuccess) return galcapi::fail_cuda(e, "destroy sync");

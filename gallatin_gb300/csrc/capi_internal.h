@@ -26,6 +26,11 @@ struct gal_allocator {
   uint64_t d_boffs_bytes;
   uint64_t *d_btable;
   uint64_t d_btable_bytes;
+  // scratch of the binned batch path: one sorted batch, bin counters
+  uint64_t *d_bsorted;
+  uint64_t d_bsorted_bytes;
+  uint32_t *d_bbins;
+  uint64_t d_bbins_bytes;
 };
 
 struct gal_veb {

@@ -195,7 +195,7 @@ __global__ void batch_kernel(A *a, const uint64_t *reqs, uint64_t n, uint64_t *t
 // between batches (which also orders a batch's table writes before the next
 // batch's frees read them)
 template <class A>
-__global__ void persistent_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets, uint32_t n_batches,
+__global__ void GALWORK_MIXED_BOUNDS persistent_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets, uint32_t n_batches,
                                           uint64_t *table, uint32_t width, unsigned long long *stats) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
@@ -205,6 +205,86 @@ __global__ void persistent_batches_kernel(A *a, const uint64_t *reqs, const uint
   for (uint32_t b = 0; b < n_batches; ++b) {
     const uint64_t hi = offsets[b + 1];
     for (uint64_t i = offsets[b] + rank; i < hi; i += nthreads) serve_request(a, reqs[i], table, width, misses);
+    grid.sync();
+  }
+  if (misses) atomicAdd(stats + STAT_MISS, misses);
+}
+
+// Bin of a request for the binned path: 0 = free, else its power-of-two size
+// class (16 B and below share bin 1; 2^27 B and above share bin 24).
+constexpr uint32_t kBins = 25;
+__device__ __forceinline__ uint32_t request_bin(uint64_t req) {
+  const uint32_t size = (uint32_t)req;
+  if (size == 0) return 0;
+  int cl = size <= 16 ? 4 : 32 - __clz((int)(size - 1));
+  if (cl > 27) cl = 27;
+  return (uint32_t)(cl - 3);
+}
+
+// Binned persistent path: each batch is first counting-sorted by bin into
+// `sorted` (capacity: the largest batch), so that the lanes of a warp ask for
+// the same class and one reservation serves the warp. Phases per batch:
+//   A  every CTA takes its bins' ranges and scatters its requests
+//   B  serve the sorted batch; count the next batch's bins
+// `bins` is 4 x kBins u32, zero at launch: counts and cursors, double
+// buffered by batch parity. Requests are dealt to CTAs the same way in the
+// count and the scatter (i = first + rank + k * threads), so the per-CTA
+// counts kept in shared memory between the two phases stay valid.
+template <class A>
+__global__ void GALWORK_MIXED_BOUNDS binned_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets,
+                                                           uint32_t n_batches, uint64_t *table, uint32_t width,
+                                                           unsigned long long *stats, uint64_t *sorted,
+                                                           uint32_t *bins) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ uint32_t s_cnt[kBins];
+  __shared__ uint32_t s_pos[kBins];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t rank = grid.thread_rank();
+  unsigned long long misses = 0;
+
+  auto count_batch = [&](uint32_t b) {
+    uint32_t *hist = bins + (b & 1) * kBins;
+    if (threadIdx.x < kBins) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t hi = offsets[b + 1];
+    for (uint64_t i = offsets[b] + rank; i < hi; i += nthreads) atomicAdd(&s_cnt[request_bin(reqs[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < kBins && s_cnt[threadIdx.x]) atomicAdd(hist + threadIdx.x, s_cnt[threadIdx.x]);
+  };
+
+  if (n_batches) count_batch(0);
+  grid.sync();
+  for (uint32_t b = 0; b < n_batches; ++b) {
+    uint32_t *hist = bins + (b & 1) * kBins;
+    uint32_t *cursor = bins + (2 + (b & 1)) * kBins;
+    // phase A: bin starts (exclusive prefix of the counts), this CTA's
+    // ranges, scatter
+    if (threadIdx.x == 0) {
+      uint32_t run = 0;
+      for (uint32_t k = 0; k < kBins; ++k) {
+        const uint32_t n = __ldcg(hist + k);
+        s_pos[k] = run;
+        run += n;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < kBins && s_cnt[threadIdx.x])
+      s_pos[threadIdx.x] += atomicAdd(cursor + threadIdx.x, s_cnt[threadIdx.x]);
+    __syncthreads();
+    const uint64_t lo = offsets[b], hi = offsets[b + 1];
+    for (uint64_t i = lo + rank; i < hi; i += nthreads) {
+      const uint64_t req = reqs[i];
+      sorted[atomicAdd(&s_pos[request_bin(req)], 1u)] = req;
+    }
+    grid.sync();
+    // phase B: serve; recycle this parity's counters; count the next batch
+    for (uint64_t j = rank; j < hi - lo; j += nthreads) serve_request(a, __ldcg(sorted + j), table, width, misses);
+    if (blockIdx.x == 0 && threadIdx.x < kBins) {
+      hist[threadIdx.x] = 0;
+      cursor[threadIdx.x] = 0;
+    }
+    if (b + 1 < n_batches) count_batch(b + 1);
     grid.sync();
   }
   if (misses) atomicAdd(stats + STAT_MISS, misses);

@@ -173,15 +173,20 @@ int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t ro
  * [offsets[b], offsets[b+1]). width (8, 16, 32) limits warp aggregation to
  * tiles of that many lanes. mode 0: one launch per batch (the plain
  * per-thread call path); mode 1: one cooperative persistent launch that
- * serves every batch with a grid barrier between batches. stats as for the
+ * serves every batch with a grid barrier between batches; mode 2: as mode 1,
+ * but each batch is first counting-sorted on the device by power-of-two size
+ * class (frees first), so a warp's lanes share a class; the sort uses
+ * scratch the handle owns, sized for the largest batch (at most 2^32-1
+ * requests). ctas_per_sm: CTAs of 256 threads per SM for modes 1 and 2
+ * (kernel geometry; 0 = as many as fit, more is refused). stats as for the
  * workloads ([0] = mallocs that returned NULL). */
 int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
-                    uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode,
+                    uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
                     unsigned long long *d_stats, void *stream);
 /* Capture the same launches once into an instantiated CUDA graph; replay it
  * with gal_graph_launch and release it with gal_graph_destroy. */
 int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
-                        uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode,
+                        uint32_t n_batches, uint64_t *d_table, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
                         unsigned long long *d_stats, void **graph_out);
 int gal_graph_launch(void *graph_exec, void *stream);
 int gal_graph_destroy(void *graph_exec);
@@ -189,7 +194,8 @@ int gal_graph_destroy(void *graph_exec);
  * the handle owns (grown on demand), runs, copies the 8 stats words back and
  * synchronises `stream`. table_slots: size of the live-set table. */
 int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_t *h_offsets, uint32_t n_batches,
-                         uint64_t table_slots, uint32_t width, uint32_t mode, uint64_t *h_stats, void *stream);
+                         uint64_t table_slots, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
+                         uint64_t *h_stats, void *stream);
 
 /* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
 

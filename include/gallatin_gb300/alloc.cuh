@@ -46,6 +46,8 @@ constexpr int kSegmentLockBit = 31;
 // warps rarely find their slot's block full
 constexpr uint32_t kRefillMark = GAL_BLOCK_SLICES * 7 / 8;
 constexpr int kAdoptCandidates = 64;
+// leader-to-group marker: the slot is full and no block can replace it
+constexpr uint32_t kNoMemBlock = 0xFFFFFFFEu;
 
 // which detached blocks request_block may pin again
 enum { ADOPT_NONE = 0, ADOPT_ROOMY = 1, ADOPT_ANY = 2 };
@@ -112,6 +114,8 @@ __device__ __forceinline__ uint32_t meta_state(uint64_t m) { return (uint32_t)(m
 __device__ __forceinline__ uint32_t meta_run(uint64_t m) { return (uint32_t)(m >> GAL_META_RUN_SHIFT) & 0xFu; }
 __device__ __forceinline__ uint32_t meta_class(uint64_t m) { return meta_tree(m) + meta_run(m); }
 __device__ __forceinline__ uint32_t meta_cursor(uint64_t m) { return (uint32_t)(m >> GAL_META_CURSOR_SHIFT); }
+// tree, state and run fields together (bits 32-45)
+__device__ __forceinline__ uint32_t meta_tag(uint64_t m) { return (uint32_t)(m >> GAL_META_TREE_SHIFT) & 0x3FFFu; }
 
 __device__ __forceinline__ void count(const gal_state_t *st, int id) {
   atomicAdd(st->counters + id, 1ull);
@@ -520,6 +524,8 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   const uint32_t nslots = st->slot_count[k];
   const uint32_t slot0 = ptx::smid() % nslots;
   uint64_t *const slots = st->slots + st->slot_offset[k];
+  // tree, state and run fields of a block pinned for this class
+  const uint32_t tag = t | (GAL_STATE_PINNED << (GAL_META_STATE_SHIFT - 32)) | (r << (GAL_META_RUN_SHIFT - 32));
   void *result = nullptr;
   bool done = false;
   uint32_t strikes = 0;  // slots found full with no block to replace them
@@ -536,7 +542,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
     uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
-    uint32_t nomem = 0;
+    bool nomem = false;
     bool refill = false;
     if (lane == (uint32_t)leader) {
       const uint64_t sv = ptx::ld_acquire(slot);
@@ -555,7 +561,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
         // the block stays usable while another leader replaces it
         uint64_t m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)need << GAL_META_CURSOR_SHIFT) | need);
         take = g_n;
-        if (meta_tree(m) != t || meta_run(m) != r || meta_state(m) != GAL_STATE_PINNED) {
+        if (meta_tag(m) != tag) {
           release_live(st, b, need);
           count(st, GAL_CTR_STALE_SLOT);
           take = 0;
@@ -567,8 +573,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           if (take > 0) {
             const uint32_t part = take * c;
             m = ptx::atom_add_acquire(st->block_meta + b, ((uint64_t)part << GAL_META_CURSOR_SHIFT) | part);
-            if (meta_tree(m) != t || meta_run(m) != r || meta_state(m) != GAL_STATE_PINNED ||
-                meta_live(m) + part > GAL_BLOCK_SLICES) {
+            if (meta_tag(m) != tag || meta_live(m) + part > GAL_BLOCK_SLICES) {
               release_live(st, b, part);
               take = 0;
             }
@@ -592,14 +597,16 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           b = GAL_EMPTY_BLOCK;
         }
       }
-      if (nomem) count(st, GAL_CTR_NOMEM);
-    }
-    nomem = __shfl_sync(grp, nomem, leader);
-    if (nomem && ++strikes >= nslots) {
-      done = true;  // every slot tried: the arena cannot serve this class now
-      continue;
+      if (nomem) {
+        count(st, GAL_CTR_NOMEM);
+        b = kNoMemBlock;  // b was empty: nothing to serve from this attempt
+      }
     }
     b = __shfl_sync(grp, b, leader);
+    if (b == kNoMemBlock) {
+      if (++strikes >= nslots) done = true;  // every slot tried: the arena cannot serve this class now
+      continue;
+    }
     if (b == GAL_EMPTY_BLOCK) continue;
     take = __shfl_sync(grp, take, leader);
 
@@ -738,7 +745,7 @@ __device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_
 
 // `width` limits warp aggregation to tiles of 8, 16 or 32 lanes (the
 // reference groups the whole coalesced warp, gallatin.cuh:883-885).
-__device__ inline void *malloc(const gal_state_t *st, uint64_t size, uint32_t width = 32) {
+__device__ __forceinline__ void *malloc(const gal_state_t *st, uint64_t size, uint32_t width = 32) {
   const size_class sc = classify(st, size);
   const uint64_t tid = veb::thread_tid();
   if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, (uint32_t)(__ffs((int)sc.count) - 1), tid, width);

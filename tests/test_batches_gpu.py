@@ -18,8 +18,10 @@ def small_trace(seed=5):
     return batch_trace(seed, n_batches=12, batch_lo=1024, batch_hi=40000)
 
 
-@pytest.mark.parametrize("persistent,width", [(False, 32), (True, 32), (True, 16), (True, 8)])
-def test_batches_serve_stream_and_restore(cuda, persistent, width):
+@pytest.mark.parametrize("persistent,binned,width",
+                         [(False, False, 32), (True, False, 32), (True, False, 16), (True, False, 8),
+                          (True, True, 32), (True, True, 8)])
+def test_batches_serve_stream_and_restore(cuda, persistent, binned, width):
     reqs, offsets, slots, info = small_trace()
     with gal.Gallatin.generate_on_device(1 << 30, 3, print_info=False) as a:
         d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
@@ -28,7 +30,7 @@ def test_batches_serve_stream_and_restore(cuda, persistent, width):
         stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
         # all but the drain batch: the table then holds the live set
         a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets[:-1], d_table.data_ptr(), stats.data_ptr(),
-                      width=width, persistent=persistent)
+                      width=width, persistent=persistent, binned=binned)
         cuda.cuda.synchronize()
         assert int(stats[0]) == 0
         table = d_table.cpu().numpy().view(np.uint64)
@@ -44,14 +46,15 @@ def test_batches_serve_stream_and_restore(cuda, persistent, width):
         d_drain = cuda.from_numpy((drain - drain[0]).view(np.int64)).cuda()
         d_reqs_drain = cuda.from_numpy(reqs[int(drain[0]):].view(np.int64).copy()).cuda()
         a.run_batches(d_reqs_drain.data_ptr(), d_drain.data_ptr(), drain - drain[0], d_table.data_ptr(),
-                      stats.data_ptr(), width=width, persistent=persistent)
+                      stats.data_ptr(), width=width, persistent=persistent, binned=binned)
         a.flush_pinned()
         cuda.cuda.synchronize()
         assert not d_table.any()
         check_restored(a)
 
 
-def test_graph_replay_repeats_the_stream(cuda):
+@pytest.mark.parametrize("binned", [False, True])
+def test_graph_replay_repeats_the_stream(cuda, binned):
     reqs, offsets, slots, info = small_trace(7)
     with gal.Gallatin.generate_on_device(1 << 30, 4, print_info=False) as a:
         d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
@@ -59,7 +62,7 @@ def test_graph_replay_repeats_the_stream(cuda):
         d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
         stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
         with a.capture_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(),
-                               stats.data_ptr(), persistent=True) as g:
+                               stats.data_ptr(), persistent=True, binned=binned) as g:
             for _ in range(3):
                 g.launch()
             cuda.cuda.synchronize()
@@ -76,6 +79,8 @@ def test_batches_host_entry_point(cuda):
         out = a.run_batches_host(reqs, offsets, slots, persistent=True)
         assert out[0] == 0
         out = a.run_batches_host(reqs, offsets, slots, persistent=False, width=16)
+        assert out[0] == 0
+        out = a.run_batches_host(reqs, offsets, slots, persistent=True, binned=True, ctas_per_sm=2)
         assert out[0] == 0
 
 
@@ -100,8 +105,8 @@ def test_reference_plain_path_on_the_same_stream(cuda):
         ref.close()
 
 
-@pytest.mark.parametrize("persistent", [False, True])
-def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent):
+@pytest.mark.parametrize("persistent,binned", [(False, False), (True, False), (True, True)])
+def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent, binned):
     """Allocations live across many batches and are freed in random order, the
     live set peaking at about half the arena in size-class bytes: no request
     may fail, and the state restores after the drain."""
@@ -116,7 +121,7 @@ def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent):
         d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
         stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
         a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(), stats.data_ptr(),
-                      persistent=persistent)
+                      persistent=persistent, binned=binned)
         cuda.cuda.synchronize()
         c = a.stats()["counters"]
         assert int(stats[0]) == 0, c
@@ -124,3 +129,28 @@ def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent):
         a.flush_pinned()
         cuda.cuda.synchronize()
         check_restored(a)
+
+
+def test_binned_path_serves_each_request_like_the_plain_path(cuda):
+    """Binning only reorders a batch: every malloc gets a block of its own
+    size class and the live set after each form is the same set of slots."""
+    reqs, offsets, slots, info = small_trace(13)
+    tables = []
+    for persistent, binned in [(False, False), (True, True)]:
+        with gal.Gallatin.generate_on_device(1 << 30, 8, print_info=False) as a:
+            d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+            d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+            d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+            stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+            a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets[:-1], d_table.data_ptr(), stats.data_ptr(),
+                          persistent=persistent, binned=binned)
+            cuda.cuda.synchronize()
+            assert int(stats[0]) == 0
+            table = d_table.cpu().numpy().view(np.uint64)
+            sizes = np.zeros(slots + 1, dtype=np.uint64)
+            for r in reqs[: int(offsets[-2])]:
+                sizes[int(r >> np.uint64(32))] = int(r & np.uint64(0xFFFFFFFF))
+            live = table != 0
+            check_live(a, table[live], sizes[live])
+            tables.append(live)
+    assert np.array_equal(tables[0], tables[1])
