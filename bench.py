@@ -39,6 +39,8 @@ sys.path.insert(0, str(REPO))
 
 GIB = 1 << 30
 MIB = 1 << 20
+REF_BATCH_PREFIX = 40
+
 WORKLOADS = {
     "mixed": dict(
         arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=4_194_304, rounds=8, block=256,
@@ -185,7 +187,7 @@ def cpu_baseline(name: str, w: dict) -> dict:
     elif name == "batches":
         from gallatin_gb300.workload import batch_trace
 
-        reqs, offsets, slots, _ = batch_trace(42, n_batches=w["batches"])
+        reqs, offsets, slots, _ = batch_trace(42, n_batches=w["batches"], batch_hi=w.get("batch_hi", 524288))
         secs, misses = oracle.cpu_replay_batches(reqs, offsets, slots, cores)
         bad = 0
         units = int(offsets[-1])
@@ -207,6 +209,48 @@ def cpu_baseline(name: str, w: dict) -> dict:
     }
 
 
+def batch_prefix_rates(torch, a, reqs, offsets, slots, w, stats, flush, steps) -> dict:
+    """This allocator on the sample the reference arm of the batching workload
+    is timed on (the first batches plus a drain): the configured persistent
+    path and the plain one-launch-per-batch path."""
+    from gallatin_gb300.workload import prefix_with_drain
+
+    preqs, poffs = prefix_with_drain(reqs, offsets, REF_BATCH_PREFIX)
+    n = int(poffs[-1])
+    d_reqs = torch.from_numpy(preqs.view(np.int64)).cuda()
+    d_offs = torch.from_numpy(poffs.view(np.int64)).cuda()
+    d_table = torch.zeros(slots + 1, dtype=torch.int64, device="cuda")
+    bargs = (d_reqs.data_ptr(), d_offs.data_ptr(), poffs, d_table.data_ptr(), stats.data_ptr())
+    out = {"sample": f"first {REF_BATCH_PREFIX} of {len(offsets) - 2} batches, then a drain batch", "requests": n}
+    stream = torch.cuda.current_stream()
+    for name, persistent in (("persistent+graph", True), ("per-thread launches", False)):
+        graph = None
+        if persistent:
+            graph = a.capture_batches(*bargs, width=w["width"], persistent=True, binned=w["binned"])
+            fn = lambda: graph.launch(stream.cuda_stream)  # noqa: E731
+        else:
+            fn = lambda: a.run_batches(*bargs, width=w["width"], persistent=False, stream=stream.cuda_stream)  # noqa: E731
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        stats.zero_()
+        times = []
+        for _ in range(steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        if graph is not None:
+            graph.close()
+        ms = sum(times) / len(times)
+        out[name] = {"value": n / (ms / 1e3), "unit": "requests/s", "ms_per_step": ms, "misses": int(stats[0].item())}
+    return out
+
+
 def run(args) -> dict | None:
     import torch
 
@@ -225,6 +269,10 @@ def run(args) -> dict | None:
         w["rounds"] = args.rounds
     if args.arena_gib:
         w["arena"] = int(args.arena_gib * GIB)
+    if args.batches and "batches" in w:
+        w["batches"] = args.batches
+    if args.batch_hi and "batches" in w:
+        w["batch_hi"] = args.batch_hi
     impl = args.impl
     if impl == "reference":
         import oracle
@@ -288,9 +336,17 @@ def run(args) -> dict | None:
             "l2": "flushed (256 MiB write) before every timed step",
         }
     elif args.workload == "batches":
-        from gallatin_gb300.workload import batch_trace
+        from gallatin_gb300.workload import batch_trace, prefix_with_drain
 
-        reqs, offsets, slots, info = batch_trace(42, n_batches=w["batches"])
+        reqs, offsets, slots, info = batch_trace(42, n_batches=w["batches"], batch_hi=w.get("batch_hi", 524288))
+        sample = None
+        if impl == "reference":
+            # The reference's plain path runs this stream's first batches at
+            # full speed, but from batch 45 its mallocs return NULL (blocks are
+            # recycled only once all 4096 slices are back) and a batch takes a
+            # minute; its arm is timed on the first 40 batches plus a drain.
+            reqs, offsets = prefix_with_drain(reqs, offsets, REF_BATCH_PREFIX)
+            sample = f"first {REF_BATCH_PREFIX} of {w['batches']} batches, then a drain batch"
         units = int(offsets[-1])
         alg_bytes = units * 8  # the live-set table entry each request writes
         d_reqs = torch.from_numpy(reqs.view(np.int64)).cuda()
@@ -315,7 +371,8 @@ def run(args) -> dict | None:
 
         h2d = units * 8 + len(offsets) * 8
         config = {
-            "workload": "batching: 64 batches of U[1k,512k] requests, lognormal(ln 256, 1.5) sizes in [16 B, 64 MiB], "
+            "workload": f"batching: {w['batches']} batches of U[1k,{w.get('batch_hi', 524288) // 1024}k] requests, "
+                        "lognormal(ln 256, 1.5) sizes in [16 B, 64 MiB], "
                         "60/40 malloc/free over the live set, then a drain batch",
             "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
             "max_size": w["max_size"], "requests": units, "mallocs": info["mallocs"], "frees": info["frees"],
@@ -325,6 +382,9 @@ def run(args) -> dict | None:
                           + (", each batch counting-sorted by size class on the device" if w["binned"] else "")),
             "l2": "flushed (256 MiB write) before every timed step",
         }
+        if sample:
+            config["sample"] = sample
+            config["requests"] = units
     else:
         n = w["threads"]
         units = n
@@ -438,6 +498,8 @@ def run(args) -> dict | None:
     }
     if args.workload == "batches" and impl == "gb300":
         graph.close()
+        if not args.no_prefix:
+            result["prefix"] = batch_prefix_rates(torch, a, reqs, offsets, slots, w, stats, flush, args.steps)
         if args.autotune:
             from gallatin_gb300.autotune import autotune_batches
 
@@ -479,6 +541,9 @@ def main() -> int:
     ap.add_argument("--rounds", type=int, default=0, help="override the rounds of the mixed workload")
     ap.add_argument("--arena-gib", type=float, default=0.0, help="override the arena size")
     ap.add_argument("--autotune", action="store_true", help="batches workload: add the segment x width sweep")
+    ap.add_argument("--batches", type=int, default=0, help="override the batch count (small profiling cases)")
+    ap.add_argument("--batch-hi", type=int, default=0, help="override the largest batch size")
+    ap.add_argument("--no-prefix", action="store_true", help="batches workload: skip the timing on the reference's sample")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     res = run(args)

@@ -183,7 +183,7 @@ __device__ __forceinline__ void serve_request(A *a, uint64_t req, uint64_t *tabl
 
 // plain path: one launch per batch, one thread per request
 template <class A>
-__global__ void batch_kernel(A *a, const uint64_t *reqs, uint64_t n, uint64_t *table, uint32_t width,
+__global__ void GALWORK_MIXED_BOUNDS batch_kernel(A *a, const uint64_t *reqs, uint64_t n, uint64_t *table, uint32_t width,
                              unsigned long long *stats) {
   const uint64_t i = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
   unsigned long long misses = 0;

@@ -136,3 +136,20 @@ def batch_trace(
         "peak_class_bytes": peak_bytes,
     }
     return reqs, np.array(offsets, dtype=np.uint64), next_slot, info
+
+
+def prefix_with_drain(reqs: np.ndarray, offsets: np.ndarray, k: int):
+    """The first k batches of a request stream, then one batch that frees every
+    slot those batches leave live, so the prefix also starts and ends with an
+    empty live set. Returns (requests, offsets)."""
+    k = min(k, len(offsets) - 1)
+    head = np.asarray(reqs[: int(offsets[k])], dtype=np.uint64)
+    slots = head >> np.uint64(32)
+    is_malloc = (head & np.uint64(0xFFFFFFFF)) != 0
+    # the last request naming a slot decides whether it is live
+    rev_slots = slots[::-1]
+    uniq, first_in_rev = np.unique(rev_slots, return_index=True)
+    live = uniq[is_malloc[::-1][first_in_rev]]
+    out = np.concatenate([head, live.astype(np.uint64) << np.uint64(32)])
+    offs = np.concatenate([np.asarray(offsets[: k + 1], dtype=np.uint64), [np.uint64(len(out))]])
+    return out, offs.astype(np.uint64)

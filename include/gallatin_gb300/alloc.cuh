@@ -38,7 +38,7 @@
 namespace gal {
 
 constexpr int kSliceAttempts = 4096;      // group attempts per slice request
-constexpr int kClaimSteps = 160;          // fetch-and steps per reservation
+constexpr int kClaimSteps = 256;          // fetch-and steps per reservation
 constexpr int kRequestBlockAttempts = 512;
 constexpr int kSegmentLockSpins = 1 << 20;
 constexpr int kSegmentLockBit = 31;
@@ -362,7 +362,7 @@ __device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uin
   const int64_t drun = (int64_t)r - (int64_t)meta_run(m);
   const uint64_t delta = (uint64_t)(dstate * (1ll << GAL_META_STATE_SHIFT)) +
                          (uint64_t)(dtree * (1ll << GAL_META_TREE_SHIFT)) +
-                         (uint64_t)(drun * (1ll << GAL_META_RUN_SHIFT)) + (uint64_t)live;
+                         (uint64_t)(drun * (1ll << GAL_META_RUN_SHIFT)) - (m & GAL_META_REUSED_BIT) + (uint64_t)live;
   ptx::atom_add_release(st->block_meta + b, delta);
 }
 
@@ -397,7 +397,8 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
     uint64_t m = ptx::ld_relaxed(st->block_meta + cand);
     for (int i = 0; i < 8; ++i) {
       if (!adopt_listed(m, k, roomy) || meta_live(m) + c > GAL_BLOCK_SLICES) break;
-      const uint64_t nm = m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
+      const uint64_t nm =
+          (m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT)) | GAL_META_REUSED_BIT;
       const uint64_t r = ptx::cas_acq_rel(st->block_meta + cand, m, nm);
       if (r == m) {
         adopt_sync_both(st, k, cand);
@@ -592,7 +593,11 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           refill = true;  // swap in another block once this group is served
         }
         if (take > 0) {
-          cursor = meta_cursor(m) & (GAL_BLOCK_SLICES - 1);
+          cursor = meta_cursor(m);
+          // a reused block's free slices are scattered: start leaders at
+          // hashed positions so they do not all chase the same word
+          if (m & GAL_META_REUSED_BIT) cursor *= 0x9E3779B1u;
+          cursor &= GAL_BLOCK_SLICES - 1;
         } else {
           b = GAL_EMPTY_BLOCK;
         }

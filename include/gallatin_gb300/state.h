@@ -50,6 +50,8 @@
  *               DETACHED (no longer pinned; recycled when live reaches 0),
  *               WHOLE (one block-tier allocation)
  *   bits 42-45  log2 of the run length the block serves (largest tree only)
+ *   bit  46     reused: pinned again while it still held slices, so its free
+ *               slices are scattered and the cursor does not point at them
  *   bits 48-63  cursor: position hint for the next claim, wraps mod 2^16
  * All transitions are atomic adds of field deltas (or a CAS for the
  * conditional retire) so concurrent reservations and their undos commute. */
@@ -57,6 +59,7 @@
 #define GAL_META_TREE_SHIFT 32
 #define GAL_META_STATE_SHIFT 40
 #define GAL_META_RUN_SHIFT 42
+#define GAL_META_REUSED_BIT (1ull << 46)
 #define GAL_META_CURSOR_SHIFT 48
 #define GAL_STATE_FREE 0u
 #define GAL_STATE_PINNED 1u
