@@ -50,6 +50,11 @@ WORKLOADS = {
     # the batching configuration: 64 batches of 1k-512k requests, lognormal
     # sizes, 60/40 malloc/free over the live set, plus a drain batch
     "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32, binned=True),
+    # the serving configuration: Poisson arrivals (2,000 streams/s at 0.5 s
+    # per 16-token step), lognormal lengths, one 8 KiB page per step, the
+    # admission gate at 80 % of a 120 GiB arena
+    "serving": dict(arena=120 * GIB, segment=16 * MIB, min_size=16, max_size=4096, steps=600, arrivals=1000.0,
+                    page_bytes=8192, slots=262144, max_pages=2048, gate=0.8),
     # the mixed workload without its 256 segment-tier requests: only the
     # slice tier runs, which is what the reference arm can be compared on
     "mixed-slices": dict(
@@ -184,6 +189,24 @@ def cpu_baseline(name: str, w: dict) -> dict:
         )
         units = n * rounds + (n // w["block"] // w["seg_every"] if w["seg_every"] else 0)
         sample = f"full workload: {n} threads x {rounds} rounds + segment-tier requests, glibc malloc/free"
+    elif name == "serving":
+        from gallatin_gb300.serving import quantile_ns
+        from gallatin_gb300.workload import serving_admission, serving_trace
+
+        trace = serving_trace(42, steps=w["steps"], arrivals_per_step=w["arrivals"])
+        budget = int(w["gate"] * w["arena"]) // w["page_bytes"]
+        admit, _ = serving_admission(trace, budget, w["slots"])
+        secs, checksums, hist, misses = oracle.cpu_replay_serving(trace, admit, page_bytes=w["page_bytes"],
+                                                                  workers=cores)
+        units = int(hist.sum())
+        return {
+            "value": units / secs, "unit": "pages/s", "cores": cores, "kind": "port",
+            "sample": f"full schedule: {w['steps']} steps, {units} page mallocs, glibc malloc/free, one worker per "
+                      "share of the active streams, a barrier per step (the reference has no CPU implementation)",
+            "seconds": secs, "misses": misses,
+            "latency_ns": {"p50": quantile_ns(hist, 0.5), "p99": quantile_ns(hist, 0.99)},
+            "_checksums": checksums,
+        }
     elif name == "batches":
         from gallatin_gb300.workload import batch_trace
 
@@ -301,7 +324,7 @@ def run(args) -> dict | None:
 
         gal.load()
 
-    unit = "requests/s" if args.workload == "batches" else "malloc+free pairs/s"
+    unit = {"batches": "requests/s", "serving": "pages/s"}.get(args.workload, "malloc+free pairs/s")
     stream = torch.cuda.current_stream()
     s_ptr = stream.cuda_stream
     a = make_allocator(impl, w)
@@ -385,6 +408,44 @@ def run(args) -> dict | None:
         if sample:
             config["sample"] = sample
             config["requests"] = units
+    elif args.workload == "serving":
+        from gallatin_gb300.serving import ServingRun
+        from gallatin_gb300.workload import serving_trace
+
+        if args.serve_steps:
+            w["steps"] = args.serve_steps
+        trace = serving_trace(42, steps=w["steps"], arrivals_per_step=w["arrivals"])
+        budget = int(w["gate"] * w["arena"]) // w["page_bytes"]
+        srv_kw = dict(budget_pages=budget, page_bytes=w["page_bytes"], max_slots=w["slots"], max_pages=w["max_pages"])
+        srv = ServingRun(torch, trace, **srv_kw)
+        persistent = impl != "reference"
+
+        def step():
+            srv.run(a.run_serving, persistent=persistent, stream=s_ptr)
+
+        def e2e_step():
+            r = ServingRun(torch, trace, **srv_kw)  # trace to the device
+            r.run(a.run_serving, persistent=persistent, stream=s_ptr)
+            res_e = r.results()  # outputs back to the host
+            out = np.zeros(8, dtype=np.uint64)
+            out[0] = res_e["step_stats"][:, 7].sum()
+            return out
+
+        n_str = len(trace["pages"])
+        h2d = (w["steps"] + 1) * 4 + n_str * 8 + (n_str + 1) * 8
+        d2h = n_str * 16 + w["steps"] * 64 + 864 * 8
+        units = None  # pages of one run, read back after the warm-up
+        config = {
+            "workload": f"serving: Poisson arrivals 2,000 streams/s, 0.5 s per step, {w['steps']} steps, "
+                        "lognormal(ln 1024, 1.0) tokens in [128, 32768], one 8 KiB page (16 tokens) per step per "
+                        "stream, pages freed at completion, admission gated at 80 % of the arena",
+            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+            "max_size": w["max_size"], "steps": w["steps"], "streams": n_str, "budget_pages": budget,
+            "slots": w["slots"], "seed": 42,
+            "path": ("reference: plain path, one launch per phase per step" if impl == "reference"
+                     else "device-resident loop: one cooperative launch for all steps"),
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
     else:
         n = w["threads"]
         units = n
@@ -405,6 +466,9 @@ def run(args) -> dict | None:
         step()
     torch.cuda.synchronize()
     stats.zero_()
+    if args.workload == "serving":
+        units = int(srv.results()["step_stats"][:, 0].sum())
+        alg_bytes = units * 256  # 16 tokens written into each page and read back
 
     times = []
     barrier(torch, world)
@@ -445,7 +509,7 @@ def run(args) -> dict | None:
             "value": units * args.steps * world / e2e_total,
             "unit": unit,
             "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": 64,
+            "d2h_bytes_per_step": d2h if args.workload == "serving" else 64,
             "ms_per_step": 1e3 * e2e_total / args.steps,
             "misses": int(e2e_bad[0]),
             "verify_failures": int(e2e_bad[1]),
@@ -472,8 +536,9 @@ def run(args) -> dict | None:
             pass
 
     result = {
-        "metric": ("malloc+free ops/s (one op = one malloc or one free request)" if args.workload == "batches"
-                   else "malloc+free ops/s (one op = one malloc + its free)"),
+        "metric": {"batches": "malloc+free ops/s (one op = one malloc or one free request)",
+                   "serving": "page allocations/s of the serving loop (p50/p99 page-malloc latency in 'serving')"
+                   }.get(args.workload, "malloc+free ops/s (one op = one malloc + its free)"),
         "value": value,
         "unit": unit,
         "n_gpus": world,
@@ -496,6 +561,34 @@ def run(args) -> dict | None:
         "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
         "step_ms": times,
     }
+    if args.workload == "serving":
+        from gallatin_gb300.serving import summarize
+        from gallatin_gb300.workload import serving_admission
+
+        res = srv.results()
+        result["serving"] = summarize(res, page_bytes=w["page_bytes"], segment_bytes=w["segment"],
+                                      seconds=ms_per_step / 1e3)
+        admit_model, _ = serving_admission(trace, budget, w["slots"])
+        result["serving"]["admission_matches_model"] = bool(np.array_equal(res["admit_step"], admit_model))
+        if impl == "gb300" and not args.no_prefix:
+            # the plain path (one launch per phase per step) on the same trace
+            srv0 = ServingRun(torch, trace, **srv_kw)
+            srv0.run(a.run_serving, persistent=False, stream=s_ptr)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            flush.fill_(1)
+            e0.record(stream)
+            srv0.run(a.run_serving, persistent=False, stream=s_ptr)
+            e1.record(stream)
+            e1.synchronize()
+            ms0 = e0.elapsed_time(e1)
+            res0 = srv0.results()
+            plain = summarize(res0, page_bytes=w["page_bytes"], segment_bytes=w["segment"], seconds=ms0 / 1e3)
+            plain["ms_per_run"] = ms0
+            plain["same_results"] = bool(np.array_equal(res0["checksum"], res["checksum"]) and
+                                         np.array_equal(res0["admit_step"], res["admit_step"]))
+            result["serving"]["plain_path"] = plain
     if args.workload == "batches" and impl == "gb300":
         graph.close()
         if not args.no_prefix:
@@ -516,6 +609,12 @@ def run(args) -> dict | None:
         result["autotune"] = result_autotune
     if rank == 0 and impl == "gb300" and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, w)
+        if args.workload == "serving":
+            # the glibc replay computes every finished stream's checksum on the
+            # host: the device must report the same ones
+            want = result["cpu_baseline"].pop("_checksums")
+            fin = res["finish_step"] != 0xFFFFFFFF
+            result["serving"]["checksum_mismatches_vs_host_replay"] = int((res["checksum"][fin] != want[fin]).sum())
     if impl == "reference":
         result["cpu_baseline"] = {
             "value": value, "unit": unit, "cores": 0, "kind": "reference",
@@ -543,7 +642,9 @@ def main() -> int:
     ap.add_argument("--autotune", action="store_true", help="batches workload: add the segment x width sweep")
     ap.add_argument("--batches", type=int, default=0, help="override the batch count (small profiling cases)")
     ap.add_argument("--batch-hi", type=int, default=0, help="override the largest batch size")
-    ap.add_argument("--no-prefix", action="store_true", help="batches workload: skip the timing on the reference's sample")
+    ap.add_argument("--no-prefix", action="store_true",
+                    help="batches: skip the timing on the reference's sample; serving: skip the plain-path run")
+    ap.add_argument("--serve-steps", type=int, default=0, help="override the serving workload's step count")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     res = run(args)

@@ -192,6 +192,7 @@ def load(path: str | Path | None = None):
         "gal_graph_launch": (i32, [vp, vp]),
         "gal_graph_destroy": (i32, [vp]),
         "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, u32, vp, vp]),
+        "gal_run_serving": (i32, [vp, vp, vp, vp, vp]),
         "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
         "gal_veb_destroy": (i32, [vp]),
         "gal_veb_num_layers": (i32, [vp]),
@@ -438,6 +439,13 @@ class Gallatin:
         _check(load().gal_run_batches_host(self.handle, ptr, offsets.ctypes.data, len(offsets) - 1, table_slots, width,
                                            _batch_mode(persistent, binned), ctas_per_sm, out.ctypes.data, stream))
         return out
+
+    # -- serving loop ---------------------------------------------------------
+    def run_serving(self, trace_ptr, params_ptr, out_ptr, stream: int = 0) -> int:
+        """gal_run_serving on this allocator (pointers to the structs of
+        gallatin_gb300.serving); returns 0 or raises GalError."""
+        _check(load().gal_run_serving(self.handle, trace_ptr, params_ptr, out_ptr, stream))
+        return 0
 
     # -- inspection -----------------------------------------------------------
     def stats(self) -> dict:

@@ -130,6 +130,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   h->d_bsorted = nullptr;
   h->d_bbins = nullptr;
   h->d_bsorted_bytes = h->d_bbins_bytes = 0;
+  h->d_serve = nullptr;
+  h->d_serve_bytes = 0;
   h->min_size = min_size;
   h->max_size = max_size;
   gal_state_t &s = h->hs;
@@ -251,6 +253,7 @@ extern "C" int gal_destroy(gal_allocator *h) {
   if (h->d_btable) cudaFree(h->d_btable);
   if (h->d_bsorted) cudaFree(h->d_bsorted);
   if (h->d_bbins) cudaFree(h->d_bbins);
+  if (h->d_serve) cudaFree(h->d_serve);
   free_all(h->device_allocs);
   delete h;
   if (e != cudaSuccess) return galcapi::fail_cuda(e, "destroy sync");

@@ -31,6 +31,9 @@ struct gal_allocator {
   uint64_t d_bsorted_bytes;
   uint32_t *d_bbins;
   uint64_t d_bbins_bytes;
+  // scratch of the serving loop: slot and page tables
+  void *d_serve;
+  uint64_t d_serve_bytes;
 };
 
 struct gal_veb {

@@ -153,3 +153,100 @@ def prefix_with_drain(reqs: np.ndarray, offsets: np.ndarray, k: int):
     out = np.concatenate([head, live.astype(np.uint64) << np.uint64(32)])
     offs = np.concatenate([np.asarray(offsets[: k + 1], dtype=np.uint64), [np.uint64(len(out))]])
     return out, offs.astype(np.uint64)
+
+
+# ---- serving ---------------------------------------------------------------
+
+def serving_trace(
+    seed: int = 42,
+    steps: int = 600,
+    arrivals_per_step: float = 1000.0,
+    median_tokens: float = 1024.0,
+    sigma: float = 1.0,
+    min_tokens: int = 128,
+    max_tokens: int = 32768,
+    tokens_per_page: int = 16,
+):
+    """Streams of the serving configuration.
+
+    Arrivals are Poisson: arrivals_per_step = rate x simulated step length
+    (2,000 streams/s x 0.5 s per 16-token step = 1,000). Stream lengths are
+    lognormal(ln median, sigma) tokens clipped to [min, max]; a stream needs
+    ceil(tokens / tokens_per_page) pages and takes one per step.
+
+    Returns a dict of numpy arrays: arrival_step (u32, ascending), tokens
+    (u32), pages (u32), page_prefix (u64, n+1: pages of streams before i),
+    arrivals_end (u32, steps+1: arrivals_end[s + 1] streams arrived at steps
+    <= s), plus steps and tokens_per_page."""
+    rng = np.random.default_rng(seed)
+    per_step = rng.poisson(arrivals_per_step, size=steps)
+    n = int(per_step.sum())
+    arrival_step = np.repeat(np.arange(steps, dtype=np.uint32), per_step)
+    tokens = np.clip(np.rint(rng.lognormal(np.log(median_tokens), sigma, size=n)), min_tokens, max_tokens).astype(np.uint32)
+    pages = ((tokens + tokens_per_page - 1) // tokens_per_page).astype(np.uint32)
+    page_prefix = np.zeros(n + 1, dtype=np.uint64)
+    np.cumsum(pages, out=page_prefix[1:])
+    arrivals_end = np.zeros(steps + 1, dtype=np.uint32)
+    np.cumsum(per_step, out=arrivals_end[1:])
+    return {"arrival_step": arrival_step, "tokens": tokens, "pages": pages, "page_prefix": page_prefix,
+            "arrivals_end": arrivals_end, "steps": steps, "tokens_per_page": tokens_per_page}
+
+
+def single_stream(trace: dict, i: int, extra_steps: int = 2) -> dict:
+    """A trace holding only stream i of `trace`, arriving at step 0, with its
+    original id (so its tokens, and its checksum, are the ones it has in the
+    full trace)."""
+    p = int(trace["pages"][i])
+    steps = p + extra_steps
+    arrivals_end = np.ones(steps + 1, dtype=np.uint32)
+    arrivals_end[0] = 0
+    return {"arrival_step": np.zeros(1, dtype=np.uint32), "tokens": trace["tokens"][i:i + 1].copy(),
+            "pages": trace["pages"][i:i + 1].copy(), "page_prefix": np.array([0, p], dtype=np.uint64),
+            "arrivals_end": arrivals_end, "steps": steps, "tokens_per_page": trace["tokens_per_page"],
+            "ids": np.array([i], dtype=np.uint32)}
+
+
+def serving_admission(trace: dict, budget_pages: int, max_slots: int):
+    """Host model of the serving loop's first-come-first-served admission (the
+    device loop must reproduce it exactly). At step s, k_s streams are
+    admitted: the largest k such that they have arrived by step s, k free slots
+    exist, and the pages committed to admitted, unfinished streams plus their
+    pages stay within budget_pages. Every admitted stream takes one page per
+    step; a stream with p pages admitted at step a finishes at step a + p - 1,
+    and its slot and pages count as free for the admission of step a + p.
+
+    Returns (admit_step u32[n], 0xFFFFFFFF = never admitted within the steps;
+    per-step arrays: admitted, committed pages after the step's admissions)."""
+    steps = trace["steps"]
+    pages = trace["pages"].astype(np.int64)
+    prefix = trace["page_prefix"]
+    arrivals_end = trace["arrivals_end"]
+    n = len(pages)
+    admit = np.full(n, 0xFFFFFFFF, dtype=np.uint32)
+    release_pages = np.zeros(steps + 2, dtype=np.int64)
+    release_slots = np.zeros(steps + 2, dtype=np.int64)
+    nxt = 0
+    committed = 0
+    free_slots = max_slots
+    out_k = np.zeros(steps, dtype=np.int64)
+    out_committed = np.zeros(steps, dtype=np.int64)
+    for s in range(steps):
+        committed -= release_pages[s]
+        free_slots += release_slots[s]
+        hi = min(int(arrivals_end[s + 1]), nxt + free_slots)
+        room = budget_pages - committed
+        lim = int(prefix[nxt]) + room
+        k = int(np.searchsorted(prefix[nxt:hi + 1], lim, side="right")) - 1 if hi > nxt else 0
+        k = max(k, 0)
+        if k:
+            admit[nxt:nxt + k] = s
+            p = pages[nxt:nxt + k]
+            committed += int(p.sum())
+            free_slots -= k
+            fin = s + p
+            np.add.at(release_pages, np.minimum(fin, steps + 1), p)
+            np.add.at(release_slots, np.minimum(fin, steps + 1), 1)
+            nxt += k
+        out_k[s] = k
+        out_committed[s] = committed
+    return admit, {"admitted": out_k, "committed": out_committed}

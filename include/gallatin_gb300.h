@@ -197,6 +197,63 @@ int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_
                          uint64_t table_slots, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
                          uint64_t *h_stats, void *stream);
 
+/* --- serving loop (no reference counterpart: the reference only serves
+ *     per-thread calls from user kernels) ---
+ * Streams arrive over simulated steps; a stream of L tokens takes one page
+ * of page_bytes per step until it holds ceil(L / tokens_per_page) pages,
+ * writing its tokens (u64 each) into each page, then reads them back into a
+ * checksum (sum of token * (2 * position + 1), mod 2^64) and frees its pages.
+ * Admission is first-come first-served on the device: at step s the longest
+ * run of waiting streams is admitted that has arrived (arrivals_end[s + 1]),
+ * fits the free slots (max_slots), and keeps the pages committed to admitted,
+ * unfinished streams within budget_pages. A stream finishing at step s frees
+ * its slot and pages for the admission of step s + 1. After the last step the
+ * unfinished streams' pages are freed, so the allocator ends as it started.
+ * mode 0: the plain path, one launch per phase per step (phase 1: a thread
+ * per stream takes its page; phase 2: finished streams return theirs);
+ * mode 1: every step in one cooperative persistent launch. */
+typedef struct gal_serve_trace_t {
+  uint32_t n_streams;
+  uint32_t pad_;
+  const uint32_t *arrivals_end; /* device [steps + 1]: [s + 1] = arrived at steps <= s */
+  const uint32_t *tokens;       /* device [n]: L per stream, arrival order */
+  const uint32_t *pages;        /* device [n]: ceil(L / tokens_per_page) <= max_pages */
+  const uint64_t *page_prefix;  /* device [n + 1]: pages of the streams before i */
+  const uint32_t *ids;          /* device [n] or NULL: the id stream i's tokens are
+                                   derived from (NULL: i), so one stream can be
+                                   replayed alone with the tokens it has in a mix */
+} gal_serve_trace_t;
+
+typedef struct gal_serve_params_t {
+  uint32_t steps;
+  uint32_t tokens_per_page;
+  uint64_t page_bytes;
+  uint64_t budget_pages; /* admission cap, e.g. 0.8 * arena / page_bytes */
+  uint64_t seed;         /* token values */
+  uint32_t max_slots;    /* streams served at once */
+  uint32_t max_pages;    /* page-table width per stream */
+  uint32_t width;        /* warp-aggregation width 8, 16 or 32 */
+  uint32_t mode;
+  uint32_t ctas_per_sm;  /* 0 = as many as fit */
+  uint32_t pad_;
+} gal_serve_params_t;
+
+#define GAL_SERVE_HIST_BUCKETS 864 /* ns < 32 exact, then 32 buckets per octave */
+#define GAL_SERVE_STATS 8          /* per step: allocated, finished, freed, live,
+                                      committed, queued, owned segments, NULLs */
+typedef struct gal_serve_out_t { /* device arrays, cleared by the call */
+  uint64_t *checksum;     /* [n], 0 for streams that did not finish */
+  uint32_t *admit_step;   /* [n], 0xFFFFFFFF = not admitted */
+  uint32_t *finish_step;  /* [n], 0xFFFFFFFF = not finished */
+  uint64_t *step_stats;   /* [steps][GAL_SERVE_STATS] */
+  uint64_t *latency_hist; /* [GAL_SERVE_HIST_BUCKETS] page-malloc latency */
+} gal_serve_out_t;
+
+/* The server's slot and page tables are scratch the handle owns (grown on
+ * demand: max_slots * max_pages * 8 bytes and a few arrays of max_slots). */
+int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *trace, const gal_serve_params_t *params,
+                    const gal_serve_out_t *out, void *stream);
+
 /* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
 
 typedef struct gal_veb_op {

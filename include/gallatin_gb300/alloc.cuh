@@ -226,7 +226,9 @@ __device__ inline void seg_avail_add_one(const gal_state_t *st, uint64_t seg) {
   }
 }
 
-// Format the smallest free segment for tree t. Caller holds tree t's lock.
+// Format the smallest free segment for tree t. Callers hold tree t's lock
+// when a segment of t has several blocks, so that concurrent requests do not
+// each format one; every step is atomic on its own.
 __device__ inline uint64_t attach_segment(const gal_state_t *st, uint32_t t) {
   const uint64_t seg = veb::malloc_first(&st->segment_tree);
   if (seg == veb::kFail) return veb::kFail;
@@ -434,12 +436,14 @@ __device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint
   for (; a < kRequestBlockAttempts; ++a) {
     uint64_t seg = veb::find_random_valid_index(sub, mix_tid(tid, a));
     if (seg == veb::kFail) {
-      if (!try_lock(st, (int)t)) {
+      // a segment of one block serves exactly one request: no lock needed
+      const bool solo = (st->blocks_per_segment >> t) == 1;
+      if (!solo && !try_lock(st, (int)t)) {
         backoff(a);
         continue;
       }
       seg = attach_segment(st, t);
-      unlock(st, (int)t);
+      if (!solo) unlock(st, (int)t);
       if (seg == veb::kFail) {
         if (veb::find_first_valid_index(sub) != veb::kFail) continue;
         break;  // no formatted segment with a free block, no free segment
@@ -677,9 +681,10 @@ __device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t 
   const uint32_t word = slice >> 6;
   const uint32_t bit = slice & 63;
   // a block of the largest tree serves one run length, kept in its meta word
-  // (stable while this allocation holds the block out of its segment)
+  // (stable while this allocation holds the block out of its segment, and
+  // written before the pointer reached this thread: a plain load suffices)
   uint32_t c = 1;
-  if (t == (uint32_t)st->num_trees - 1) c = 1u << meta_run(ptx::ld_relaxed(st->block_meta + b));
+  if (t == (uint32_t)st->num_trees - 1) c = 1u << meta_run(st->block_meta[b]);
   const uint64_t mask = ((c >= 64) ? ~0ull : ((1ull << c) - 1)) << bit;
   const uint32_t lane = ptx::laneid();
 
@@ -766,7 +771,10 @@ __device__ inline void free(const gal_state_t *st, void *ptr, uint32_t width = 3
     return;
   }
   const uint64_t seg = off >> st->segment_shift;
-  const uint16_t id = ptx::ld_relaxed(st->chunk_ids + seg);
+  // the segment's tag cannot change while the allocation is live, and it was
+  // set before the pointer was handed out, so a plain (L1-cacheable) load
+  // sees it (freeing a pointer twice is undefined, as in the reference)
+  const uint16_t id = st->chunk_ids[seg];
   if (id < (uint16_t)st->num_trees) {
     free_slice(st, seg, id, off & (st->segment_bytes - 1), width);
   } else if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees) {

@@ -89,6 +89,11 @@ def load_replay():
         lib.cpu_replay_batches.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_int, POINTER(c_uint64)]
         lib.cpu_mixed_classes.restype = None
         lib.cpu_mixed_classes.argtypes = [c_uint64, c_uint32, c_uint64, c_void_p]
+        lib.cpu_serving_checksums.restype = None
+        lib.cpu_serving_checksums.argtypes = [c_uint64, c_void_p, c_uint64, c_void_p, c_int]
+        lib.cpu_replay_serving.restype = c_double
+        lib.cpu_replay_serving.argtypes = [c_uint64, c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_uint64,
+                                           c_uint64, c_int, c_void_p, c_void_p, POINTER(c_uint64)]
         _REPLAY = lib
     return _REPLAY
 
@@ -117,6 +122,32 @@ def cpu_replay_batches(reqs: np.ndarray, offsets: np.ndarray, table_slots: int, 
     secs = load_replay().cpu_replay_batches(reqs.ctypes.data, offsets.ctypes.data, len(offsets) - 1,
                                             table.ctypes.data, workers, ctypes.byref(misses))
     return secs, misses.value
+
+
+def serving_checksums(tokens: np.ndarray, seed: int, workers: int = 1) -> np.ndarray:
+    """The checksum each stream of a serving trace must report when it
+    finishes (sum of token * (2 * position + 1) mod 2^64)."""
+    tokens = np.ascontiguousarray(tokens, dtype=np.uint32)
+    out = np.zeros(len(tokens), dtype=np.uint64)
+    load_replay().cpu_serving_checksums(len(tokens), tokens.ctypes.data, seed, out.ctypes.data, workers)
+    return out
+
+
+def cpu_replay_serving(trace: dict, admit_step: np.ndarray, *, page_bytes: int = 8192, seed: int = 42,
+                       workers: int = 1):
+    """glibc malloc/free through the serving schedule; returns (seconds,
+    checksums, latency histogram, NULL count)."""
+    tokens = np.ascontiguousarray(trace["tokens"], dtype=np.uint32)
+    pages = np.ascontiguousarray(trace["pages"], dtype=np.uint32)
+    admit = np.ascontiguousarray(admit_step, dtype=np.uint32)
+    n = len(tokens)
+    checksum = np.zeros(max(n, 1), dtype=np.uint64)
+    hist = np.zeros(864, dtype=np.uint64)
+    nulls = c_uint64(0)
+    secs = load_replay().cpu_replay_serving(n, tokens.ctypes.data, pages.ctypes.data, admit.ctypes.data,
+                                            int(trace["steps"]), int(trace["tokens_per_page"]), page_bytes, seed,
+                                            workers, checksum.ctypes.data, hist.ctypes.data, ctypes.byref(nulls))
+    return secs, checksum[:n], hist, nulls.value
 
 
 def cpu_replay_pairs(n, size, workers=1):
@@ -163,6 +194,7 @@ def _bind_ref(lib):
         "galref_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "galref_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "galref_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, vp]),
+        "galref_run_serving": (i32, [vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -238,6 +270,11 @@ class RefGallatin:
         if self._lib.galref_run_batches(self._h, d_reqs, d_offsets, offsets.ctypes.data, len(offsets) - 1, d_table,
                                         1 if persistent else 0, d_stats, stream) != 0:
             raise RuntimeError("galref_run_batches failed")
+
+    def run_serving(self, trace_ptr, params_ptr, out_ptr, stream=0):
+        """The serving loop's plain path (one launch per phase per step) over
+        the reference allocator; the params' mode is ignored."""
+        return self._lib.galref_run_serving(self._h, trace_ptr, params_ptr, out_ptr, stream)
 
     def close(self):
         if self._h:

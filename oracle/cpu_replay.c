@@ -228,3 +228,201 @@ double cpu_replay_batches(const uint64_t *reqs, const uint64_t *offsets, uint32_
   free(th);
   return t1 - t0;
 }
+
+/* ---- serving ------------------------------------------------------------
+ * Token `pos` of stream `id` and the checksum a finished stream reports
+ * (gallatin_gb300/csrc/serving.cuh): sum of token * (2 * pos + 1) mod 2^64. */
+static uint64_t serve_token(uint64_t seed, uint32_t id, uint32_t pos) {
+  return splitmix64(seed ^ (((uint64_t)id << 16) | pos));
+}
+
+typedef struct {
+  uint64_t begin, end, seed;
+  const uint32_t *tokens;
+  uint64_t *out;
+} sum_job;
+
+static void *run_sums(void *arg) {
+  sum_job *j = (sum_job *)arg;
+  for (uint64_t i = j->begin; i < j->end; ++i) {
+    uint64_t acc = 0;
+    for (uint32_t p = 0; p < j->tokens[i]; ++p) acc += serve_token(j->seed, (uint32_t)i, p) * (2ull * p + 1);
+    j->out[i] = acc;
+  }
+  return NULL;
+}
+
+void cpu_serving_checksums(uint64_t n, const uint32_t *tokens, uint64_t seed, uint64_t *out, int workers) {
+  if (workers < 1) workers = 1;
+  if (workers > 256) workers = 256;
+  sum_job jobs[256];
+  pthread_t th[256];
+  for (int w = 0; w < workers; ++w) {
+    jobs[w].begin = n * (uint64_t)w / (uint64_t)workers;
+    jobs[w].end = n * (uint64_t)(w + 1) / (uint64_t)workers;
+    jobs[w].seed = seed;
+    jobs[w].tokens = tokens;
+    jobs[w].out = out;
+    pthread_create(&th[w], NULL, run_sums, &jobs[w]);
+  }
+  for (int w = 0; w < workers; ++w) pthread_join(th[w], NULL);
+}
+
+/* Latency bucket of the serving histogram: ns < 32 exact, then 32 linear
+ * buckets per octave (864 buckets). */
+static uint32_t serve_bucket(uint64_t ns) {
+  if (ns < 32) return (uint32_t)ns;
+  int e = 63 - __builtin_clzll(ns);
+  if (e > 30) return 863;
+  return 32u + (uint32_t)(e - 5) * 32u + ((uint32_t)(ns >> (e - 5)) & 31u);
+}
+
+typedef struct serve_shared serve_shared;
+typedef struct {
+  serve_shared *sh;
+  int w;
+  uint64_t hist[864];
+} serve_worker;
+
+struct serve_shared {
+  uint32_t steps, tokens_per_page, workers;
+  uint64_t page_bytes, seed, n;
+  const uint32_t *tokens, *pages;
+  const uint64_t *step_begin; /* streams admitted at step s: [step_begin[s], step_begin[s+1]) */
+  uint64_t *checksum;
+  void ***table;  /* per stream: its pages */
+  uint32_t *held; /* per stream */
+  uint32_t *active;
+  uint64_t n_active;
+  uint8_t *done;
+  uint64_t nulls;
+  pthread_barrier_t bar;
+};
+
+static void *serve_run(void *arg) {
+  serve_worker *wk = (serve_worker *)arg;
+  serve_shared *sh = wk->sh;
+  uint64_t nulls = 0;
+  for (uint32_t s = 0; s < sh->steps; ++s) {
+    if (wk->w == 0) {
+      /* compact survivors, then append this step's admissions */
+      uint64_t m = 0;
+      for (uint64_t i = 0; i < sh->n_active; ++i)
+        if (!sh->done[sh->active[i]]) sh->active[m++] = sh->active[i];
+      for (uint64_t id = sh->step_begin[s]; id < sh->step_begin[s + 1]; ++id) {
+        sh->table[id] = (void **)malloc(sizeof(void *) * sh->pages[id]);
+        sh->held[id] = 0;
+        sh->active[m++] = (uint32_t)id;
+      }
+      sh->n_active = m;
+    }
+    pthread_barrier_wait(&sh->bar);
+    const uint64_t lo = sh->n_active * (uint64_t)wk->w / sh->workers;
+    const uint64_t hi = sh->n_active * (uint64_t)(wk->w + 1) / sh->workers;
+    for (uint64_t i = lo; i < hi; ++i) {
+      const uint32_t id = sh->active[i];
+      struct timespec t0, t1;
+      clock_gettime(CLOCK_MONOTONIC, &t0);
+      uint64_t *p = (uint64_t *)malloc(sh->page_bytes);
+      clock_gettime(CLOCK_MONOTONIC, &t1);
+      wk->hist[serve_bucket((uint64_t)(t1.tv_sec - t0.tv_sec) * 1000000000ull + (uint64_t)(t1.tv_nsec - t0.tv_nsec))]++;
+      if (!p) {
+        nulls++;
+        continue;
+      }
+      const uint32_t j = sh->held[id];
+      const uint32_t base = j * sh->tokens_per_page;
+      const uint32_t len = sh->tokens[id];
+      const uint32_t cnt = len - base < sh->tokens_per_page ? len - base : sh->tokens_per_page;
+      for (uint32_t t = 0; t < cnt; ++t) p[t] = serve_token(sh->seed, id, base + t);
+      sh->table[id][j] = p;
+      sh->held[id] = j + 1;
+      if (j + 1 == sh->pages[id]) {
+        uint64_t acc = 0;
+        for (uint32_t q = 0; q <= j; ++q) {
+          const uint64_t *pg = (const uint64_t *)sh->table[id][q];
+          const uint32_t b = q * sh->tokens_per_page;
+          const uint32_t c = len - b < sh->tokens_per_page ? len - b : sh->tokens_per_page;
+          for (uint32_t t = 0; t < c; ++t) acc += pg[t] * (2ull * (b + t) + 1);
+          free((void *)pg);
+        }
+        sh->checksum[id] = acc;
+        free(sh->table[id]);
+        sh->table[id] = NULL;
+        sh->done[id] = 1;
+      }
+    }
+    pthread_barrier_wait(&sh->bar);
+  }
+  __atomic_fetch_add(&sh->nulls, nulls, __ATOMIC_RELAXED);
+  return NULL;
+}
+
+/* glibc malloc/free through the serving schedule: admit_step[i] (from the
+ * admission model) says when stream i starts; a worker per contiguous share
+ * of the active streams takes each stream's page per step, a barrier closes
+ * the step. Unfinished streams are freed after the last step (untimed).
+ * Returns wall seconds of the steps; hist gets the per-malloc latency. */
+double cpu_replay_serving(uint64_t n, const uint32_t *tokens, const uint32_t *pages, const uint32_t *admit_step,
+                          uint32_t steps, uint32_t tokens_per_page, uint64_t page_bytes, uint64_t seed, int workers,
+                          uint64_t *checksum, uint64_t *hist, uint64_t *nulls) {
+  if (workers < 1) workers = 1;
+  if (workers > 256) workers = 256;
+  serve_shared sh;
+  memset(&sh, 0, sizeof(sh));
+  sh.steps = steps;
+  sh.tokens_per_page = tokens_per_page;
+  sh.workers = (uint32_t)workers;
+  sh.page_bytes = page_bytes;
+  sh.seed = seed;
+  sh.n = n;
+  sh.tokens = tokens;
+  sh.pages = pages;
+  sh.checksum = checksum;
+  uint64_t *step_begin = (uint64_t *)calloc(steps + 1, sizeof(uint64_t));
+  /* admissions are first come first served: stream ids admitted at step s
+   * form one run, after those of earlier steps */
+  uint64_t id = 0;
+  for (uint32_t s = 0; s < steps; ++s) {
+    step_begin[s] = id;
+    while (id < n && admit_step[id] == s) ++id;
+  }
+  step_begin[steps] = id;
+  sh.step_begin = step_begin;
+  sh.table = (void ***)calloc(n ? n : 1, sizeof(void **));
+  sh.held = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
+  sh.active = (uint32_t *)calloc(n ? n : 1, sizeof(uint32_t));
+  sh.done = (uint8_t *)calloc(n ? n : 1, 1);
+  for (uint64_t i = 0; i < n; ++i) checksum[i] = 0;
+  pthread_barrier_init(&sh.bar, NULL, (unsigned)workers);
+  serve_worker *wk = (serve_worker *)calloc((size_t)workers, sizeof(serve_worker));
+  pthread_t *th = (pthread_t *)calloc((size_t)workers, sizeof(pthread_t));
+  const double t0 = now_s();
+  for (int w = 0; w < workers; ++w) {
+    wk[w].sh = &sh;
+    wk[w].w = w;
+    pthread_create(&th[w], NULL, serve_run, &wk[w]);
+  }
+  for (int w = 0; w < workers; ++w) pthread_join(th[w], NULL);
+  const double t1 = now_s();
+  for (int b = 0; b < 864; ++b) {
+    hist[b] = 0;
+    for (int w = 0; w < workers; ++w) hist[b] += wk[w].hist[b];
+  }
+  for (uint64_t i = 0; i < n; ++i) {
+    if (sh.table[i]) {
+      for (uint32_t q = 0; q < sh.held[i]; ++q) free(sh.table[i][q]);
+      free(sh.table[i]);
+    }
+  }
+  *nulls = sh.nulls;
+  pthread_barrier_destroy(&sh.bar);
+  free(step_begin);
+  free(sh.table);
+  free(sh.held);
+  free(sh.active);
+  free(sh.done);
+  free(wk);
+  free(th);
+  return t1 - t0;
+}

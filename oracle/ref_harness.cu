@@ -15,7 +15,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
-#include "gallatin_gb300.h"  // gal_veb_op layout and op codes only
+#include "gallatin_gb300.h"  // gal_veb_op layout, op codes and serving structs only
+#include "serving.cuh"
 #include "workloads.cuh"
 
 using namespace gallatin::allocators;
@@ -75,6 +76,8 @@ struct RefAlloc {
   uint8_t *d_classes;
   uint64_t d_classes_bytes;
   unsigned long long *d_stats;
+  void *d_serve;
+  uint64_t d_serve_bytes;
 };
 
 int config_of(uint64_t seg, uint64_t mn, uint64_t mx) {
@@ -132,9 +135,45 @@ int launch_batches(void *dev, const uint64_t *d_reqs, const uint64_t *d_offsets,
                             width, stats) == cudaSuccess ? 0 : 2;
 }
 
+template <class G>
+int launch_serving(void *dev, const galserve::server_t &sv, const galserve::trace_t &t, const galserve::params_t &p,
+                   const galserve::out_t &o, cudaStream_t s) {
+  int dev_id = 0;
+  cudaDeviceProp prop;
+  cudaGetDevice(&dev_id);
+  cudaGetDeviceProperties(&prop, dev_id);
+  // the plain path (mode 0): one launch per phase per step
+  return galserve::run((G *)dev, sv, t, p, o, 0, 4u * prop.multiProcessorCount, s) == cudaSuccess ? 0 : 2;
+}
+
 }  // namespace
 
 extern "C" {
+
+int galref_run_serving(void *h, const gal_serve_trace_t *tr, const gal_serve_params_t *pr, const gal_serve_out_t *out,
+                       void *stream) {
+  RefAlloc *a = (RefAlloc *)h;
+  const galserve::layout_t l = galserve::layout(pr->max_slots, pr->max_pages);
+  if (l.total > a->d_serve_bytes) {
+    if (a->d_serve) cudaFree(a->d_serve);
+    a->d_serve = nullptr;
+    a->d_serve_bytes = 0;
+    if (cudaMalloc(&a->d_serve, l.total) != cudaSuccess) return 3;
+    a->d_serve_bytes = l.total;
+  }
+  const galserve::server_t sv = galserve::server_at(a->d_serve, pr->max_slots, pr->max_pages);
+  galserve::trace_t t{tr->n_streams, tr->arrivals_end, tr->tokens, tr->pages, tr->page_prefix, tr->ids};
+  galserve::params_t p{pr->steps, pr->tokens_per_page, pr->page_bytes, pr->budget_pages, pr->seed, 32};
+  galserve::out_t o{out->checksum, out->admit_step, out->finish_step, out->step_stats,
+                    (unsigned long long *)out->latency_hist};
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a->config) {
+    case 0: return launch_serving<ref_16m_16_4096>(a->dev, sv, t, p, o, s);
+    case 1: return launch_serving<ref_16m_128_4096>(a->dev, sv, t, p, o, s);
+    case 2: return launch_serving<ref_64m_16_4096>(a->dev, sv, t, p, o, s);
+    default: return launch_serving<ref_4m_16_1024>(a->dev, sv, t, p, o, s);
+  }
+}
 
 int galref_run_batches(void *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
                        uint32_t n_batches, uint64_t *d_table, uint32_t mode, unsigned long long *d_stats,
@@ -199,6 +238,8 @@ int galref_create(uint64_t max_bytes, uint64_t seed, uint64_t seg, uint64_t mn, 
   a->config = config;
   a->d_classes = nullptr;
   a->d_classes_bytes = 0;
+  a->d_serve = nullptr;
+  a->d_serve_bytes = 0;
   switch (config) {
     case 0: a->dev = ref_16m_16_4096::generate_on_device(max_bytes, seed, false); break;
     case 1: a->dev = ref_16m_128_4096::generate_on_device(max_bytes, seed, false); break;
@@ -221,6 +262,7 @@ int galref_destroy(void *h) {
     default: ref_4m_16_1024::free_on_device((ref_4m_16_1024 *)a->dev); break;
   }
   if (a->d_classes) cudaFree(a->d_classes);
+  if (a->d_serve) cudaFree(a->d_serve);
   cudaFree(a->d_stats);
   delete a;
   return 0;
