@@ -155,8 +155,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   // Pinned blocks per slot class: one per SM for small trees; for large
   // trees as many as a quarter of the arena split evenly over the trees
   // affords (a block of tree t is 4096 slices of min << t bytes). A run
-  // class of 2^r slices of the largest tree gets that tree's count >> r (at
-  // least 2): its requests are rarer. Slots are filled on first use, so a
+  // class of 2^r slices of the largest tree gets that tree's count >> (r - 1)
+  // (at least 2): longer runs are asked for more rarely. Slots are filled on first use, so a
   // class that is never asked for pins nothing.
   if (min_slots == 0) min_slots = 4;
   const uint64_t budget = s.arena_bytes / (4ull * (uint64_t)num_trees);
@@ -167,7 +167,7 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
     uint64_t c = budget / block_bytes;
     if (c > s.num_sms) c = s.num_sms;
     if (c < min_slots) c = min_slots;
-    if ((int)k >= num_trees) c = (c >> (k - (uint32_t)num_trees + 1)) > 2 ? (c >> (k - (uint32_t)num_trees + 1)) : 2;
+    if ((int)k > num_trees) c = (c >> (k - (uint32_t)num_trees)) > 2 ? (c >> (k - (uint32_t)num_trees)) : 2;
     s.slot_count[k] = (uint32_t)c;
     s.slot_offset[k] = total;
     total += (uint32_t)c;

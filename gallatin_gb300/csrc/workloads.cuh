@@ -61,7 +61,7 @@ __device__ __forceinline__ ulonglong2 load_cg(const ulonglong2 *p) {
 }
 
 template <class Alloc>
-__global__ void __launch_bounds__(1024) pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
+__global__ void __launch_bounds__(1024, 1) pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
   const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
   if (tid >= n) return;
   uint64_t *p = (uint64_t *)alloc->malloc(size);

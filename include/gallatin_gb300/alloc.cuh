@@ -46,8 +46,10 @@ constexpr int kSegmentLockBit = 31;
 // warps rarely find their slot's block full
 constexpr uint32_t kRefillMark = GAL_BLOCK_SLICES * 7 / 8;
 constexpr int kAdoptCandidates = 64;
-// leader-to-group marker: the slot is full and no block can replace it
+// leader-to-group markers: the slot is full and no block can replace it;
+// the slot cannot serve while another leader replaces its block
 constexpr uint32_t kNoMemBlock = 0xFFFFFFFEu;
+constexpr uint32_t kBusyBlock = 0xFFFFFFFDu;
 
 // which detached blocks request_block may pin again
 enum { ADOPT_NONE = 0, ADOPT_ROOMY = 1, ADOPT_ANY = 2 };
@@ -534,6 +536,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   void *result = nullptr;
   bool done = false;
   uint32_t strikes = 0;  // slots found full with no block to replace them
+  uint32_t hops = 0;     // slots passed over while another leader replaced their block
   for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
     const uint32_t grp = __ballot_sync(peers, !done);
     if (grp == 0) break;
@@ -542,12 +545,13 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     const uint32_t g_n = __popc(grp);
     const uint32_t g_rank = __popc(grp & lt);
     const uint32_t need = g_n * c;
-    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3) + strikes) % nslots;
+    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3) + strikes + hops) % nslots;
 
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
     uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
     bool nomem = false;
+    bool busy = false;
     bool refill = false;
     if (lane == (uint32_t)leader) {
       const uint64_t sv = ptx::ld_acquire(slot);
@@ -559,7 +563,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           nomem = replace_slot(st, slot, sv, t, r, tid, ADOPT_ANY, &b) == REPLACE_NOMEM;
         } else {
           count(st, GAL_CTR_SLOT_BUSY);
-          backoff(attempt);
+          busy = true;
         }
       }
       if (b != GAL_EMPTY_BLOCK) {
@@ -590,7 +594,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
               nomem = replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ANY, &nb) == REPLACE_NOMEM;
             } else {
               count(st, GAL_CTR_SLOT_BUSY);
-              backoff(attempt);
+              busy = true;
             }
           }
         } else if (!replacing && meta_live(m) + need > kRefillMark) {
@@ -609,11 +613,19 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
       if (nomem) {
         count(st, GAL_CTR_NOMEM);
         b = kNoMemBlock;  // b was empty: nothing to serve from this attempt
+      } else if (busy) {
+        // try the next slot now; wait only after passing over all of them
+        if ((hops + 1) % nslots == 0) backoff(attempt);
+        b = kBusyBlock;
       }
     }
     b = __shfl_sync(grp, b, leader);
     if (b == kNoMemBlock) {
       if (++strikes >= nslots) done = true;  // every slot tried: the arena cannot serve this class now
+      continue;
+    }
+    if (b == kBusyBlock) {
+      ++hops;
       continue;
     }
     if (b == GAL_EMPTY_BLOCK) continue;
