@@ -54,7 +54,10 @@ WORKLOADS = {
     # per 16-token step), lognormal lengths, one 8 KiB page per step, the
     # admission gate at 80 % of a 120 GiB arena
     "serving": dict(arena=120 * GIB, segment=16 * MIB, min_size=16, max_size=4096, steps=600, arrivals=1000.0,
-                    page_bytes=8192, slots=262144, max_pages=2048, gate=0.8),
+                    page_bytes=8192, slots=262144, max_pages=2048, gate=0.8,
+                    # one CTA per SM: CTAs left idle in a step wait at the grid
+                    # barrier and slow the working ones (measured 1-4 per SM)
+                    ctas_per_sm=1),
     # the mixed workload without its 256 segment-tier requests: only the
     # slice tier runs, which is what the reference arm can be compared on
     "mixed-slices": dict(
@@ -420,12 +423,14 @@ def run(args) -> dict | None:
         srv = ServingRun(torch, trace, **srv_kw)
         persistent = impl != "reference"
 
+        geo = w["ctas_per_sm"] if persistent else 0
+
         def step():
-            srv.run(a.run_serving, persistent=persistent, stream=s_ptr)
+            srv.run(a.run_serving, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
 
         def e2e_step():
             r = ServingRun(torch, trace, **srv_kw)  # trace to the device
-            r.run(a.run_serving, persistent=persistent, stream=s_ptr)
+            r.run(a.run_serving, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
             res_e = r.results()  # outputs back to the host
             out = np.zeros(8, dtype=np.uint64)
             out[0] = res_e["step_stats"][:, 7].sum()
@@ -433,7 +438,7 @@ def run(args) -> dict | None:
 
         n_str = len(trace["pages"])
         h2d = (w["steps"] + 1) * 4 + n_str * 8 + (n_str + 1) * 8
-        d2h = n_str * 16 + w["steps"] * 64 + 864 * 8
+        d2h = n_str * 16 + w["steps"] * 80 + 864 * 8
         units = None  # pages of one run, read back after the warm-up
         config = {
             "workload": f"serving: Poisson arrivals 2,000 streams/s, 0.5 s per step, {w['steps']} steps, "
@@ -443,7 +448,7 @@ def run(args) -> dict | None:
             "max_size": w["max_size"], "steps": w["steps"], "streams": n_str, "budget_pages": budget,
             "slots": w["slots"], "seed": 42,
             "path": ("reference: plain path, one launch per phase per step" if impl == "reference"
-                     else "device-resident loop: one cooperative launch for all steps"),
+                     else f"device-resident loop: one cooperative launch for all steps, {w['ctas_per_sm']} CTA/SM"),
             "l2": "flushed (256 MiB write) before every timed step",
         }
     else:

@@ -8,8 +8,9 @@
 //
 // Step s, phase 1: every active stream, and the k_s streams admitted at this
 // step, allocates its next page (one thread each; the malloc is timed with
-// %globaltimer). Phase 2: one CTA per stream that completed in phase 1 reads
-// its pages, frees them and returns its slot; thread 0 computes k_{s+1}: the
+// %globaltimer). Phase 2: the pages of the streams that completed in phase 1
+// are read back and freed, a page per thread, and their slots returned;
+// thread 0 computes k_{s+1}: the
 // longest arrival-ordered run of waiting streams that have arrived, fit in
 // the free slots, and whose pages fit in the page budget beside the pages
 // committed to admitted, unfinished streams. Admission therefore needs no
@@ -79,16 +80,18 @@ struct ctrl_t {
   uint64_t committed;   // pages of admitted, unfinished streams
   uint64_t live;        // pages held
   uint64_t act_n;       // active streams carried into this step
-  uint64_t done_n;      // streams that completed in this step's phase 1
-  uint64_t done_pages;  // their pages
-  uint64_t misses;      // page mallocs that returned NULL in phase 1
-  uint64_t pad[7];
+  uint64_t done_packed;  // (streams << 40) | pages of the streams that completed in phase 1
+  uint64_t misses;       // page mallocs that returned NULL in phase 1
+  uint64_t t_phase1;     // %globaltimer when this step's phase 1 began
+  uint64_t t_phase2;     // ... and when its phase 2 began
+  uint64_t pad[6];
 };
 
 struct server_t {
   ctrl_t *ctrl;           // [2]
   uint32_t *act;          // [2][slots] active slot lists
   uint32_t *done_list;    // [slots]
+  uint32_t *done_off;     // [slots] first page of each finished stream in the step's flat page list
   uint32_t *free_stack;   // [slots]
   uint32_t *slot_stream;  // [slots]
   uint32_t *slot_pages;   // [slots] pages held
@@ -101,12 +104,12 @@ struct out_t {
   uint64_t *checksum;        // [n] over the tokens read back at completion
   uint32_t *admit_step;      // [n]
   uint32_t *finish_step;     // [n]
-  uint64_t *step_stats;      // [steps][8]
+  uint64_t *step_stats;      // [steps][kStats]
   unsigned long long *hist;  // [kHistBuckets] page-malloc latency, ns
 };
 
 enum { STAT_ALLOC = 0, STAT_DONE = 1, STAT_FREED = 2, STAT_LIVE = 3, STAT_COMMITTED = 4, STAT_QUEUED = 5,
-       STAT_OWNED_SEGMENTS = 6, STAT_MISSES = 7 };
+       STAT_OWNED_SEGMENTS = 6, STAT_MISSES = 7, STAT_PHASE1_NS = 8, STAT_PHASE2_NS = 9, kStats = 10 };
 
 // Segments the allocator holds (formatted or in multi-segment allocations),
 // when it can say; ~0 otherwise.
@@ -170,9 +173,13 @@ __device__ inline void take_page(A *a, const server_t &sv, const trace_t &tr, co
   }
   sv.slot_pages[slot] = j;
   if (j == npages) {
-    const uint64_t idx = atomicAdd((unsigned long long *)&sv.ctrl[par].done_n, 1ull);
+    // one atomic hands out the stream's index and the offset of its pages, so
+    // the offsets rise with the index
+    const uint64_t packed =
+        atomicAdd((unsigned long long *)&sv.ctrl[par].done_packed, (1ull << 40) | (unsigned long long)npages);
+    const uint64_t idx = packed >> 40;
     sv.done_list[idx] = slot;
-    atomicAdd((unsigned long long *)&sv.ctrl[par].done_pages, (unsigned long long)npages);
+    sv.done_off[idx] = (uint32_t)(packed & ((1ull << 40) - 1));
   } else {
     const uint64_t idx = atomicAdd((unsigned long long *)&sv.ctrl[par ^ 1].act_n, 1ull);
     sv.act[(uint64_t)(par ^ 1) * sv.slots + idx] = slot;
@@ -184,6 +191,11 @@ __device__ inline void phase1(A *a, const server_t &sv, const trace_t &tr, const
                               uint32_t s, uint64_t rank, uint64_t nthreads, uint32_t *s_hist) {
   const ctrl_t &c = sv.ctrl[s & 1];
   const uint64_t n = c.act_n, k = c.k, free_count = c.free_count, next = c.next;
+  if (rank == 0) {
+    const uint64_t t = globaltimer();
+    sv.ctrl[s & 1].t_phase1 = t;
+    if (s > 0) out.step_stats[(uint64_t)(s - 1) * kStats + STAT_PHASE2_NS] = t - sv.ctrl[(s & 1) ^ 1].t_phase2;
+  }
   for (uint64_t i = rank; i < n + k; i += nthreads) {
     if (i < n) {
       const uint32_t slot = sv.act[(uint64_t)(s & 1) * sv.slots + i];
@@ -221,44 +233,71 @@ __device__ inline uint64_t release_pages(A *a, const server_t &sv, const params_
   return acc;
 }
 
+// Finished streams' pages as one flat list, spread over every thread: page f
+// belongs to the finished stream whose first page is the last done_off <= f.
+// Each thread reads back its page's tokens, adds them to the stream's
+// checksum (a sum mod 2^64, so the order of the adds does not matter) and
+// frees the page; the thread with a stream's first page returns its slot.
 template <class A>
-__device__ inline void phase2(A *a, const server_t &sv, const trace_t &tr, const params_t &pr, const out_t &out,
-                              uint32_t s, uint64_t rank, uint64_t *s_red) {
-  const uint32_t par = s & 1;
-  const ctrl_t &c = sv.ctrl[par];
-  const uint64_t base = c.free_count - c.k;  // free-stack top after this step's pops
-  const uint64_t done = c.done_n;
-  for (uint64_t j = blockIdx.x; j < done; j += gridDim.x) {  // one CTA per finished stream
-    const uint32_t slot = sv.done_list[j];
+__device__ inline void release_flat(A *a, const server_t &sv, const trace_t &tr, const params_t &pr,
+                                    const out_t &out, uint32_t s, uint64_t done, uint64_t pages, uint64_t base,
+                                    uint64_t rank, uint64_t nthreads) {
+  for (uint64_t f = rank; f < pages; f += nthreads) {
+    uint64_t lo = 0, hi = done - 1;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi + 1) >> 1;
+      if (sv.done_off[mid] <= f) lo = mid;
+      else hi = mid - 1;
+    }
+    const uint32_t slot = sv.done_list[lo];
     const uint32_t stream = sv.slot_stream[slot];
-    const uint64_t sum = release_pages(a, sv, pr, slot, tr.tokens[stream], sv.slot_pages[slot], true, s_red);
-    if (threadIdx.x == 0) {
-      out.checksum[stream] = sum;
+    const uint32_t j = (uint32_t)(f - sv.done_off[lo]);
+    const uint64_t *p = (const uint64_t *)sv.page_table[(uint64_t)slot * sv.max_pages + j];
+    const uint32_t len = tr.tokens[stream];
+    const uint32_t first = j * pr.tokens_per_page;
+    const uint32_t cnt = len - first < pr.tokens_per_page ? len - first : pr.tokens_per_page;
+    uint64_t acc = 0;
+    for (uint32_t t = 0; t < cnt; ++t) acc += p[t] * (2ull * (first + t) + 1);
+    atomicAdd((unsigned long long *)out.checksum + stream, (unsigned long long)acc);
+    galwork::wl_free(a, (void *)p, pr.width, 0);
+    if (j == 0) {
       out.finish_step[stream] = s;
-      sv.slot_stream[slot] = kEmpty;
-      sv.free_stack[base + j] = slot;
+      sv.free_stack[base + lo] = slot;
     }
   }
+}
+
+template <class A>
+__device__ inline void phase2(A *a, const server_t &sv, const trace_t &tr, const params_t &pr, const out_t &out,
+                              uint32_t s, uint64_t rank, uint64_t nthreads) {
+  const uint32_t par = s & 1;
+  const uint64_t t2 = rank == 0 ? globaltimer() : 0;  // phase 2 begins
+  const ctrl_t &c = sv.ctrl[par];
+  const uint64_t base = c.free_count - c.k;  // free-stack top after this step's pops
+  const uint64_t packed = c.done_packed;
+  const uint64_t done = packed >> 40, done_pages = packed & ((1ull << 40) - 1);
+  if (done) release_flat(a, sv, tr, pr, out, s, done, done_pages, base, rank, nthreads);
   if (rank == 0) {
     ctrl_t &nc = sv.ctrl[par ^ 1];
     const uint64_t alloc = c.act_n + c.k - c.misses;
     nc.next = c.next + c.k;
-    nc.free_count = base + c.done_n;
-    nc.live = c.live + alloc - c.done_pages;
-    const uint64_t committed = c.committed - c.done_pages;
+    nc.free_count = base + done;
+    nc.live = c.live + alloc - done_pages;
+    const uint64_t committed = c.committed - done_pages;
     const uint64_t arrived = tr.arrivals_end[s + 1 < pr.steps ? s + 2 : pr.steps];
     uint64_t kmax = arrived > nc.next ? arrived - nc.next : 0;
     if (kmax > nc.free_count) kmax = nc.free_count;
     const uint64_t room = pr.budget_pages > committed ? pr.budget_pages - committed : 0;
     nc.k = s + 1 < pr.steps ? admit_count(tr.page_prefix, nc.next, kmax, room) : 0;
     nc.committed = committed + (tr.page_prefix[nc.next + nc.k] - tr.page_prefix[nc.next]);
-    nc.done_n = 0;
-    nc.done_pages = 0;
+    nc.done_packed = 0;
     nc.misses = 0;
-    uint64_t *st = out.step_stats + (uint64_t)s * 8;
+    sv.ctrl[par].t_phase2 = t2;
+    uint64_t *st = out.step_stats + (uint64_t)s * kStats;
+    st[STAT_PHASE1_NS] = t2 - c.t_phase1;
     st[STAT_ALLOC] = alloc;
-    st[STAT_DONE] = c.done_n;
-    st[STAT_FREED] = c.done_pages;
+    st[STAT_DONE] = done;
+    st[STAT_FREED] = done_pages;
     st[STAT_LIVE] = c.live + alloc;
     st[STAT_COMMITTED] = c.committed;
     st[STAT_QUEUED] = tr.arrivals_end[s + 1] - (c.next + c.k);
@@ -314,7 +353,7 @@ __global__ void GALWORK_MIXED_BOUNDS serve_persistent_kernel(A *a, server_t sv, 
   for (uint32_t s = 0; s < pr.steps; ++s) {
     phase1(a, sv, tr, pr, out, s, rank, nthreads, s_hist);
     grid.sync();
-    phase2(a, sv, tr, pr, out, s, rank, s_red);
+    phase2(a, sv, tr, pr, out, s, rank, nthreads);
     grid.sync();
   }
   drain(a, sv, tr, pr, s_red);
@@ -341,9 +380,8 @@ __global__ void GALWORK_MIXED_BOUNDS serve_phase1_kernel(A *a, server_t sv, trac
 template <class A>
 __global__ void GALWORK_MIXED_BOUNDS serve_phase2_kernel(A *a, server_t sv, trace_t tr, params_t pr, out_t out,
                                                          uint32_t s) {
-  __shared__ uint64_t s_red[32];
   const uint64_t rank = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  phase2(a, sv, tr, pr, out, s, rank, s_red);
+  phase2(a, sv, tr, pr, out, s, rank, (uint64_t)gridDim.x * blockDim.x);
 }
 
 template <class A>
@@ -355,7 +393,7 @@ __global__ void GALWORK_MIXED_BOUNDS serve_drain_kernel(A *a, server_t sv, trace
 // ---- host side: scratch layout, initialisation, launch ----------------------
 
 struct layout_t {
-  uint64_t ctrl, act, done_list, free_stack, slot_stream, slot_pages, page_table, total;
+  uint64_t ctrl, act, done_list, done_off, free_stack, slot_stream, slot_pages, page_table, total;
 };
 
 inline uint64_t align256(uint64_t x) { return (x + 255) & ~255ull; }
@@ -368,6 +406,8 @@ inline layout_t layout(uint32_t slots, uint32_t max_pages) {
   l.act = o;
   o = align256(o + 2ull * slots * 4);
   l.done_list = o;
+  o = align256(o + (uint64_t)slots * 4);
+  l.done_off = o;
   o = align256(o + (uint64_t)slots * 4);
   l.free_stack = o;
   o = align256(o + (uint64_t)slots * 4);
@@ -388,6 +428,7 @@ inline server_t server_at(void *base, uint32_t slots, uint32_t max_pages) {
   sv.ctrl = (ctrl_t *)(b + l.ctrl);
   sv.act = (uint32_t *)(b + l.act);
   sv.done_list = (uint32_t *)(b + l.done_list);
+  sv.done_off = (uint32_t *)(b + l.done_off);
   sv.free_stack = (uint32_t *)(b + l.free_stack);
   sv.slot_stream = (uint32_t *)(b + l.slot_stream);
   sv.slot_pages = (uint32_t *)(b + l.slot_pages);
@@ -411,7 +452,7 @@ __global__ void init_kernel(server_t sv, out_t out, uint32_t n_streams, uint32_t
     out.admit_step[i] = kEmpty;
     out.finish_step[i] = kEmpty;
   }
-  for (uint64_t i = rank; i < (uint64_t)steps * 8; i += nthreads) out.step_stats[i] = 0;
+  for (uint64_t i = rank; i < (uint64_t)steps * kStats; i += nthreads) out.step_stats[i] = 0;
   for (uint64_t i = rank; i < (uint64_t)kHistBuckets; i += nthreads) out.hist[i] = 0;
   if (rank < 2 * sizeof(ctrl_t) / 8) ((uint64_t *)sv.ctrl)[rank] = 0;
 }

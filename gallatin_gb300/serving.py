@@ -14,8 +14,9 @@ from ctypes import c_uint32, c_uint64, c_void_p
 import numpy as np
 
 HIST_BUCKETS = 864
-STATS = 8
-STAT_NAMES = ("allocated", "finished", "freed", "live", "committed", "queued", "owned_segments", "misses")
+STATS = 10
+STAT_NAMES = ("allocated", "finished", "freed", "live", "committed", "queued", "owned_segments", "misses",
+              "phase1_ns", "phase2_ns")
 NOT_SET = 0xFFFFFFFF
 
 
@@ -158,6 +159,9 @@ def summarize(res: dict, *, page_bytes: int, segment_bytes: int, seconds: float 
         "peak_live_pages": int(st[:, 3].max(initial=0)),
         "peak_committed_pages": int(st[:, 4].max(initial=0)),
         "final_queue": int(st[-1, 5]) if len(st) else 0,
+        "step_us": {"phase1_mean": float(st[:, 8].mean() / 1e3) if len(st) else 0.0,
+                    "phase2_mean": float(st[:-1, 9].mean() / 1e3) if len(st) > 1 else 0.0,
+                    "phase1_max": float(st[:, 8].max(initial=0) / 1e3)},
     }
     owned = st[:, 6]
     if len(st) and owned.max() < 2**60:

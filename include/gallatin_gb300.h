@@ -239,8 +239,10 @@ typedef struct gal_serve_params_t {
 } gal_serve_params_t;
 
 #define GAL_SERVE_HIST_BUCKETS 864 /* ns < 32 exact, then 32 buckets per octave */
-#define GAL_SERVE_STATS 8          /* per step: allocated, finished, freed, live,
-                                      committed, queued, owned segments, NULLs */
+#define GAL_SERVE_STATS 10         /* per step: allocated, finished, freed, live,
+                                      committed, queued, owned segments, NULLs,
+                                      phase-1 ns, phase-2 ns (%globaltimer, from
+                                      the start of one phase to the next) */
 typedef struct gal_serve_out_t { /* device arrays, cleared by the call */
   uint64_t *checksum;     /* [n], 0 for streams that did not finish */
   uint32_t *admit_step;   /* [n], 0xFFFFFFFF = not admitted */
