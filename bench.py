@@ -50,6 +50,11 @@ WORKLOADS = {
     # the batching configuration: 64 batches of 1k-512k requests, lognormal
     # sizes, 60/40 malloc/free over the live set, plus a drain batch
     "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32, binned=True),
+    # the data-structure configuration: a chained hash table of 64M keys
+    # (insert all, erase half, reinsert them) with 120 B nodes from a 128 B
+    # minimum allocator, and 1M doubling vectors
+    "table": dict(arena=32 * GIB, segment=16 * MIB, min_size=128, max_size=4096, keys=1 << 26, buckets=1 << 24),
+    "vectors": dict(arena=32 * GIB, segment=16 * MIB, min_size=128, max_size=4096, vectors=1_000_000),
     # the serving configuration: Poisson arrivals (2,000 streams/s at 0.5 s
     # per 16-token step), lognormal lengths, one 8 KiB page per step, the
     # admission gate at 80 % of a 120 GiB arena
@@ -192,6 +197,21 @@ def cpu_baseline(name: str, w: dict) -> dict:
         )
         units = n * rounds + (n // w["block"] // w["seg_every"] if w["seg_every"] else 0)
         sample = f"full workload: {n} threads x {rounds} rounds + segment-tier requests, glibc malloc/free"
+    elif name == "table":
+        secs, bad = oracle.cpu_table(w["keys"], w["buckets"], 9, 42, cores)
+        units = w["keys"] * 2
+        return {"value": units / secs, "unit": "key ops/s", "cores": cores, "kind": "port", "seconds": secs,
+                "misses": bad,
+                "sample": f"full workload: {w['keys']} keys insert, half erase, empty-node compaction, half "
+                          "reinsert; glibc nodes, atomic CAS, one worker per key range"}
+    elif name == "vectors":
+        from gallatin_gb300.workload import vector_lengths
+
+        lengths = vector_lengths(w["vectors"])
+        secs, bad, pushes = oracle.cpu_vectors(lengths, 1, cores)
+        return {"value": pushes / secs, "unit": "pushes/s", "cores": cores, "kind": "port", "seconds": secs,
+                "misses": bad,
+                "sample": f"full workload: {w['vectors']} vectors grown by doubling with glibc malloc/copy/free"}
     elif name == "serving":
         from gallatin_gb300.serving import quantile_ns
         from gallatin_gb300.workload import serving_admission, serving_trace
@@ -327,7 +347,8 @@ def run(args) -> dict | None:
 
         gal.load()
 
-    unit = {"batches": "requests/s", "serving": "pages/s"}.get(args.workload, "malloc+free pairs/s")
+    unit = {"batches": "requests/s", "serving": "pages/s", "table": "key ops/s", "vectors": "pushes/s"}.get(
+        args.workload, "malloc+free pairs/s")
     stream = torch.cuda.current_stream()
     s_ptr = stream.cuda_stream
     a = make_allocator(impl, w)
@@ -411,6 +432,92 @@ def run(args) -> dict | None:
         if sample:
             config["sample"] = sample
             config["requests"] = units
+    elif args.workload == "table":
+        from gallatin_gb300.workload import splitmix64
+
+        n, nb = w["keys"], w["buckets"]
+        units = n * 2  # n inserts, n/2 erases, n/2 reinserts
+        alg_bytes = units * 16  # a key and its value per op
+        ops = ["insert", "erase_half", "compact", "reinsert_half", "clear"]
+        if impl == "reference":
+            heads = torch.zeros(nb, dtype=torch.int64, device="cuda")
+            from gallatin_gb300 import TABLE_OPS
+
+            def run_ops(names, d_keys=None, st=stats):
+                for op in names:
+                    a.table_op(heads.data_ptr(), nb, 9, TABLE_OPS[op], n, st.data_ptr(), d_keys=d_keys,
+                               stream=s_ptr)
+        else:
+            tbl = a.table(nb, seed=9)
+
+            def run_ops(names, d_keys=None, st=stats):
+                for op in names:
+                    tbl.op(op, n, st.data_ptr(), d_keys=d_keys, stream=s_ptr)
+
+        def step():
+            run_ops(ops)
+
+        with np.errstate(over="ignore"):
+            h_keys = torch.from_numpy(splitmix64(np.arange(n, dtype=np.uint64) + np.uint64(42)).view(np.int64))
+        h_keys = h_keys.pin_memory()
+        d_keys_buf = torch.empty(n, dtype=torch.int64, device="cuda")
+        e2e_stats = torch.zeros(8, dtype=torch.int64, device="cuda")
+        h_stats = torch.zeros(8, dtype=torch.int64).pin_memory()
+
+        def e2e_step():
+            e2e_stats.zero_()
+            d_keys_buf.copy_(h_keys, non_blocking=True)
+            run_ops(ops, d_keys=d_keys_buf.data_ptr(), st=e2e_stats)
+            h_stats.copy_(e2e_stats, non_blocking=True)
+            torch.cuda.synchronize()
+            out = np.zeros(8, dtype=np.uint64)
+            out[0] = h_stats[0].item() + h_stats[1].item()
+            return out
+
+        h2d = n * 8
+        config = {
+            "workload": f"chained hash table: {n} uniform u64 keys (splitmix64 from seed 42), insert all, erase a "
+                        "random half, compact empty nodes, reinsert the half, free all; 120 B nodes",
+            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+            "max_size": w["max_size"], "keys": n, "buckets": nb, "seed": 42,
+            "path": "one thread per key, nodes from the allocator under test",
+            "l2": "flushed (256 MiB write) before every timed step; table state exceeds L2",
+        }
+    elif args.workload == "vectors":
+        from gallatin_gb300.workload import vector_lengths
+
+        lengths = vector_lengths(w["vectors"])
+        units = int(lengths.sum())
+        alg_bytes = units * 8  # 4 B per push plus about 4 B copied per push over the doublings
+        d_len = torch.from_numpy(lengths.view(np.int32)).cuda()
+        h_len = torch.from_numpy(lengths.view(np.int32)).pin_memory()
+        d_len_e2e = torch.empty_like(d_len)
+
+        def step():
+            a.run_vectors(d_len.data_ptr(), len(lengths), stats.data_ptr(), stream=s_ptr)
+
+        e2e_stats = torch.zeros(8, dtype=torch.int64, device="cuda")
+        h_stats = torch.zeros(8, dtype=torch.int64).pin_memory()
+
+        def e2e_step():
+            e2e_stats.zero_()
+            d_len_e2e.copy_(h_len, non_blocking=True)
+            a.run_vectors(d_len_e2e.data_ptr(), len(lengths), e2e_stats.data_ptr(), stream=s_ptr)
+            h_stats.copy_(e2e_stats, non_blocking=True)
+            torch.cuda.synchronize()
+            out = np.zeros(8, dtype=np.uint64)
+            out[0] = h_stats[0].item()
+            out[1] = h_stats[2].item()
+            return out
+
+        h2d = len(lengths) * 4
+        config = {
+            "workload": f"{len(lengths)} per-thread u32 vectors grown by push_back to lognormal(ln 64, 1.5) "
+                        "lengths capped at 65,536, doubling by malloc/copy/free, then checked and freed",
+            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+            "max_size": w["max_size"], "vectors": len(lengths), "pushes": units, "seed": 42,
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
     elif args.workload == "serving":
         from gallatin_gb300.serving import ServingRun
         from gallatin_gb300.workload import serving_trace
@@ -542,7 +649,9 @@ def run(args) -> dict | None:
 
     result = {
         "metric": {"batches": "malloc+free ops/s (one op = one malloc or one free request)",
-                   "serving": "page allocations/s of the serving loop (p50/p99 page-malloc latency in 'serving')"
+                   "serving": "page allocations/s of the serving loop (p50/p99 page-malloc latency in 'serving')",
+                   "table": "chained hash table key ops/s (insert + erase + reinsert, nodes from the allocator)",
+                   "vectors": "vector push_back/s (doubling backings from the allocator)",
                    }.get(args.workload, "malloc+free ops/s (one op = one malloc + its free)"),
         "value": value,
         "unit": unit,
@@ -566,6 +675,18 @@ def run(args) -> dict | None:
         "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
         "step_ms": times,
     }
+    if args.workload == "table":
+        # untimed check of the whole lifecycle: every key where it should be
+        chk = torch.zeros(8, dtype=torch.int64, device="cuda")
+        run_ops(["insert", "erase_half", "query_after_erase", "compact", "reinsert_half", "query", "clear"], st=chk)
+        c = chk.cpu().numpy()
+        result["checks"] = {"insert_failures": int(c[0]), "membership_errors": int(c[1]), "wrong_values": int(c[2])}
+        result["verify_failures"] = int(c[1] + c[2])
+        if impl == "gb300":
+            tbl.close()
+    if args.workload == "vectors":
+        result["verify_failures"] = int(st[2])
+        result["checks"] = {"pushes": int(st[4]), "expected_pushes": units * args.steps}
     if args.workload == "serving":
         from gallatin_gb300.serving import summarize
         from gallatin_gb300.workload import serving_admission

@@ -193,6 +193,11 @@ def load(path: str | Path | None = None):
         "gal_graph_destroy": (i32, [vp]),
         "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, u32, vp, vp]),
         "gal_run_serving": (i32, [vp, vp, vp, vp, vp]),
+        "gal_table_create": (i32, [vp, u64, u64, POINTER(vp)]),
+        "gal_table_op": (i32, [vp, u32, vp, u64, u64, vp, vp]),
+        "gal_table_chain_stats": (i32, [vp, POINTER(u64), POINTER(u64)]),
+        "gal_table_destroy": (i32, [vp]),
+        "gal_run_vectors": (i32, [vp, vp, u64, u32, vp, vp]),
         "gal_veb_create": (i32, [u64, u64, POINTER(vp)]),
         "gal_veb_destroy": (i32, [vp]),
         "gal_veb_num_layers": (i32, [vp]),
@@ -447,6 +452,17 @@ class Gallatin:
         _check(load().gal_run_serving(self.handle, trace_ptr, params_ptr, out_ptr, stream))
         return 0
 
+    # -- data structures ------------------------------------------------------
+    def table(self, nbuckets: int, seed: int = 42) -> "Table":
+        """A chained hash table whose nodes come from this allocator."""
+        h = c_void_p()
+        _check(load().gal_table_create(self.handle, nbuckets, seed, ctypes.byref(h)))
+        return Table(h.value, nbuckets)
+
+    def run_vectors(self, d_lengths: int, n: int, d_stats: int, *, start: int = 1, stream: int = 0) -> None:
+        """n per-thread doubling vectors grown to d_lengths[v] items (gal_run_vectors)."""
+        _check(load().gal_run_vectors(self.handle, d_lengths, n, start, d_stats, stream))
+
     # -- inspection -----------------------------------------------------------
     def stats(self) -> dict:
         s = _Stats()
@@ -488,6 +504,40 @@ class Gallatin:
         which = DUMP[kind][0]
         n = load().gal_veb_layer_count(self.handle, which, max(tree, 0))
         return [self.dump(kind, max(tree, 0), i) for i in range(n)]
+
+
+TABLE_OPS = {"insert": 0, "erase_half": 1, "reinsert_half": 2, "query": 3, "compact": 4, "clear": 5,
+             "query_after_erase": 6}
+DS_STATS = ("no_node", "membership", "wrong_value", "nodes_freed", "pushes")
+
+
+class Table:
+    """gal_table: a chained hash table over an allocator (gal_table_*)."""
+
+    def __init__(self, handle: int, nbuckets: int):
+        self._t = handle
+        self.nbuckets = nbuckets
+
+    def op(self, name: str, n: int, d_stats: int, *, d_keys: int | None = None, key_seed: int = 42,
+           stream: int = 0) -> None:
+        _check(load().gal_table_op(self._t, TABLE_OPS[name], d_keys, n, key_seed, d_stats, stream))
+
+    def chain_stats(self) -> tuple[int, int]:
+        """(longest chain, total nodes)."""
+        mx, tot = c_uint64(0), c_uint64(0)
+        _check(load().gal_table_chain_stats(self._t, ctypes.byref(mx), ctypes.byref(tot)))
+        return mx.value, tot.value
+
+    def close(self) -> None:
+        if self._t:
+            _check(load().gal_table_destroy(self._t))
+            self._t = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class Graph:

@@ -250,3 +250,13 @@ def serving_admission(trace: dict, budget_pages: int, max_slots: int):
         out_k[s] = k
         out_committed[s] = committed
     return admit, {"admitted": out_k, "committed": out_committed}
+
+
+# ---- data structures ---------------------------------------------------------
+
+def vector_lengths(n: int = 1_000_000, median: float = 64.0, sigma: float = 1.5, cap: int = 65536,
+                   seed: int = 42) -> np.ndarray:
+    """Target lengths of the per-thread vectors: lognormal(ln median, sigma)
+    rounded, clipped to [1, cap] (u32)."""
+    rng = np.random.default_rng(seed)
+    return np.clip(np.rint(rng.lognormal(np.log(median), sigma, size=n)), 1, cap).astype(np.uint32)

@@ -256,6 +256,43 @@ typedef struct gal_serve_out_t { /* device arrays, cleared by the call */
 int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *trace, const gal_serve_params_t *params,
                     const gal_serve_out_t *out, void *stream);
 
+/* --- allocator-backed data structures (reference data_structs/
+ *     chaining_table.cuh:57-327 and single_vector.cuh:50-200) ---
+ * A chained hash table of u64 keys and values: buckets hold chains of 120 B
+ * nodes (7 keys, 7 values, next) taken from this allocator with malloc when a
+ * chain is full; the bucket is MurmurHash64A(key, seed) mod nbuckets. The
+ * device template is galds::chaining_table in gallatin_gb300/structures.cuh;
+ * these calls run it over a batch of keys, one thread per key (or per bucket
+ * for COMPACT and CLEAR). Keys come from d_keys, or when d_keys is NULL are
+ * splitmix64(key_seed + i); the value of a key is splitmix64(key). Key i is in
+ * the "half" when splitmix64(key_seed ^ i * 0x9E3779B97F4A7C15) is odd.
+ * stats (device, 8 x u64): [0] inserts that got no node (allocator NULL),
+ * [1] keys found where absent or absent where expected, [2] wrong values,
+ * [3] nodes freed (COMPACT, CLEAR), [4] vector pushes. Erase is an addition:
+ * the reference table has none. */
+typedef struct gal_table gal_table;
+#define GAL_TABLE_INSERT 0
+#define GAL_TABLE_ERASE_HALF 1
+#define GAL_TABLE_REINSERT_HALF 2
+#define GAL_TABLE_QUERY 3            /* every key must be present */
+#define GAL_TABLE_COMPACT 4          /* unlink and free nodes left with no key */
+#define GAL_TABLE_CLEAR 5            /* free every node */
+#define GAL_TABLE_QUERY_AFTER_ERASE 6 /* present unless in the half */
+int gal_table_create(gal_allocator *h, uint64_t nbuckets, uint64_t seed, gal_table **out);
+int gal_table_op(gal_table *t, uint32_t op, const uint64_t *d_keys, uint64_t n, uint64_t key_seed,
+                 unsigned long long *d_stats, void *stream);
+/* longest chain and total nodes (reference print_chain_stats, chaining_table.cuh:300-325) */
+int gal_table_chain_stats(gal_table *t, uint64_t *max_len, uint64_t *total_nodes);
+/* frees the bucket directory; CLEAR first, or the nodes stay allocated */
+int gal_table_destroy(gal_table *t);
+/* n per-thread vectors of u32 (galds::svector): vector v starts with a
+ * backing of `start` items (rounded up to a power of two) and pushes
+ * d_lengths[v] items (v * 2654435761 + i) mod 2^32, doubling its backing
+ * (malloc, copy, free) when full; then checks every item and frees the
+ * backing. stats: [0] mallocs that returned NULL, [2] wrong items, [4] pushes. */
+int gal_run_vectors(gal_allocator *h, const uint32_t *d_lengths, uint64_t n, uint32_t start,
+                    unsigned long long *d_stats, void *stream);
+
 /* --- standalone vEB tree (reference veb_tree, veb.cuh:528-1228) --- */
 
 typedef struct gal_veb_op {

@@ -89,6 +89,10 @@ def load_replay():
         lib.cpu_replay_batches.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_int, POINTER(c_uint64)]
         lib.cpu_mixed_classes.restype = None
         lib.cpu_mixed_classes.argtypes = [c_uint64, c_uint32, c_uint64, c_void_p]
+        lib.cpu_table.restype = c_double
+        lib.cpu_table.argtypes = [c_uint64, c_uint64, c_uint64, c_uint64, c_int, POINTER(c_uint64)]
+        lib.cpu_vectors.restype = c_double
+        lib.cpu_vectors.argtypes = [c_void_p, c_uint64, c_uint32, c_int, POINTER(c_uint64), POINTER(c_uint64)]
         lib.cpu_serving_checksums.restype = None
         lib.cpu_serving_checksums.argtypes = [c_uint64, c_void_p, c_uint64, c_void_p, c_int]
         lib.cpu_replay_serving.restype = c_double
@@ -122,6 +126,23 @@ def cpu_replay_batches(reqs: np.ndarray, offsets: np.ndarray, table_slots: int, 
     secs = load_replay().cpu_replay_batches(reqs.ctypes.data, offsets.ctypes.data, len(offsets) - 1,
                                             table.ctypes.data, workers, ctypes.byref(misses))
     return secs, misses.value
+
+
+def cpu_table(n: int, nbuckets: int, table_seed: int = 9, key_seed: int = 42, workers: int = 1):
+    """glibc chained table: insert, erase half, compact, reinsert (timed);
+    returns (seconds, failures)."""
+    bad = c_uint64(0)
+    secs = load_replay().cpu_table(n, nbuckets, table_seed, key_seed, workers, ctypes.byref(bad))
+    return secs, bad.value
+
+
+def cpu_vectors(lengths: np.ndarray, start: int = 1, workers: int = 1):
+    """glibc doubling vectors; returns (seconds, failures, pushes)."""
+    lengths = np.ascontiguousarray(lengths, dtype=np.uint32)
+    bad, pushes = c_uint64(0), c_uint64(0)
+    secs = load_replay().cpu_vectors(lengths.ctypes.data, len(lengths), start, workers, ctypes.byref(bad),
+                                     ctypes.byref(pushes))
+    return secs, bad.value, pushes.value
 
 
 def serving_checksums(tokens: np.ndarray, seed: int, workers: int = 1) -> np.ndarray:
@@ -195,6 +216,8 @@ def _bind_ref(lib):
         "galref_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "galref_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, vp]),
         "galref_run_serving": (i32, [vp, vp, vp, vp, vp]),
+        "galref_table_op": (i32, [vp, vp, u64, u64, u32, vp, u64, u64, vp, vp]),
+        "galref_run_vectors": (i32, [vp, vp, u64, u32, vp, vp]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -275,6 +298,16 @@ class RefGallatin:
         """The serving loop's plain path (one launch per phase per step) over
         the reference allocator; the params' mode is ignored."""
         return self._lib.galref_run_serving(self._h, trace_ptr, params_ptr, out_ptr, stream)
+
+    def table_op(self, heads_ptr, nbuckets, seed, op, n, d_stats, *, d_keys=None, key_seed=42, stream=0):
+        """The chained table of gallatin_gb300/structures.cuh over the reference allocator."""
+        if self._lib.galref_table_op(self._h, heads_ptr, nbuckets, seed, op, d_keys, n, key_seed, d_stats,
+                                     stream) != 0:
+            raise RuntimeError("galref_table_op failed")
+
+    def run_vectors(self, d_lengths, n, d_stats, *, start=1, stream=0):
+        if self._lib.galref_run_vectors(self._h, d_lengths, n, start, d_stats, stream) != 0:
+            raise RuntimeError("galref_run_vectors failed")
 
     def close(self):
         if self._h:

@@ -426,3 +426,215 @@ double cpu_replay_serving(uint64_t n, const uint32_t *tokens, const uint32_t *pa
   free(th);
   return t1 - t0;
 }
+
+/* ---- allocator-backed data structures -------------------------------------
+ * The chained hash table and the doubling vectors of
+ * gallatin_gb300/structures.cuh with glibc malloc/free for nodes and
+ * backings, on host threads: same node shape (next, 7 keys, 7 values), same
+ * bucket (MurmurHash64A of the key mod nbuckets, as the reference table does,
+ * chaining_table.cuh:235), same keys (splitmix64(seed + i)), values
+ * (splitmix64(key)) and erased half, same vector items and doubling. */
+static uint64_t ds_murmur(uint64_t key, uint64_t seed) {
+  /* MurmurHash64A of one 8-byte key (reference hashers/murmurhash.cuh:20-61) */
+  const uint64_t m = 0xc6a4a7935bd1e995ull;
+  const int r = 47;
+  uint64_t h = seed ^ (8 * m);
+  uint64_t k = key;
+  k *= m;
+  k ^= k >> r;
+  k *= m;
+  h ^= k;
+  h *= m;
+  h ^= h >> r;
+  h *= m;
+  h ^= h >> r;
+  return h;
+}
+
+#define DS_EMPTY (~0ull)
+typedef struct ds_node {
+  struct ds_node *next;
+  uint64_t keys[7];
+  uint64_t vals[7];
+} ds_node;
+
+typedef struct {
+  ds_node **heads;
+  uint64_t nbuckets, tseed, kseed, begin, end;
+  int op; /* 0 insert, 1 erase half, 2 reinsert half, 3 query all, 4 compact, 5 clear */
+  uint64_t bad;
+} ds_job;
+
+static int ds_half(uint64_t seed, uint64_t i) { return (int)(splitmix64(seed ^ (i * 0x9E3779B97F4A7C15ull)) & 1); }
+
+static int ds_insert(ds_job *j, uint64_t key, uint64_t val) {
+  ds_node **link = j->heads + ds_murmur(key, j->tseed) % j->nbuckets;
+  ds_node *b = __atomic_load_n(link, __ATOMIC_ACQUIRE);
+  for (int hop = 0; hop < (1 << 16); ++hop) {
+    if (!b) {
+      ds_node *nb = (ds_node *)malloc(sizeof(ds_node));
+      if (!nb) return 0;
+      nb->next = NULL;
+      for (int i = 0; i < 7; ++i) nb->keys[i] = DS_EMPTY;
+      ds_node *expect = NULL;
+      if (__atomic_compare_exchange_n(link, &expect, nb, 0, __ATOMIC_ACQ_REL, __ATOMIC_ACQUIRE)) {
+        b = nb;
+      } else {
+        free(nb);
+        b = expect;
+      }
+    }
+    for (int i = 0; i < 7; ++i) {
+      uint64_t e = DS_EMPTY;
+      if (__atomic_load_n(&b->keys[i], __ATOMIC_RELAXED) == DS_EMPTY &&
+          __atomic_compare_exchange_n(&b->keys[i], &e, key, 0, __ATOMIC_ACQ_REL, __ATOMIC_RELAXED)) {
+        b->vals[i] = val;
+        return 1;
+      }
+    }
+    link = &b->next;
+    b = __atomic_load_n(link, __ATOMIC_ACQUIRE);
+  }
+  return 0;
+}
+
+static void *ds_run(void *arg) {
+  ds_job *j = (ds_job *)arg;
+  uint64_t bad = 0;
+  for (uint64_t i = j->begin; i < j->end; ++i) {
+    if (j->op == 4 || j->op == 5) {
+      ds_node **link = j->heads + i;
+      while (*link) {
+        ds_node *b = *link;
+        int empty = 1;
+        for (int q = 0; q < 7; ++q) empty &= b->keys[q] == DS_EMPTY;
+        if (j->op == 5 || empty) {
+          *link = b->next;
+          free(b);
+        } else {
+          link = &b->next;
+        }
+      }
+      continue;
+    }
+    const uint64_t key = splitmix64(j->kseed + i);
+    const int half = ds_half(j->kseed, i);
+    if (j->op == 0 || (j->op == 2 && half)) {
+      bad += !ds_insert(j, key, splitmix64(key));
+    } else if (j->op == 1 && half) {
+      int found = 0;
+      for (ds_node *b = j->heads[ds_murmur(key, j->tseed) % j->nbuckets]; b && !found; b = b->next)
+        for (int q = 0; q < 7 && !found; ++q) {
+          uint64_t e = key;
+          if (b->keys[q] == key &&
+              __atomic_compare_exchange_n(&b->keys[q], &e, DS_EMPTY, 0, __ATOMIC_ACQ_REL, __ATOMIC_RELAXED))
+            found = 1;
+        }
+      bad += !found;
+    } else if (j->op == 3) {
+      int found = 0;
+      for (ds_node *b = j->heads[ds_murmur(key, j->tseed) % j->nbuckets]; b && !found; b = b->next)
+        for (int q = 0; q < 7 && !found; ++q)
+          if (b->keys[q] == key) found = b->vals[q] == splitmix64(key) ? 1 : 2;
+      bad += found != 1;
+    }
+  }
+  j->bad = bad;
+  return NULL;
+}
+
+/* Insert n keys, erase half, compact, reinsert the half (timed), then check
+ * every key (untimed) and free every node. Returns the timed seconds; *bad
+ * counts failed inserts, missing erases and wrong or missing keys. */
+double cpu_table(uint64_t n, uint64_t nbuckets, uint64_t tseed, uint64_t kseed, int workers, uint64_t *bad) {
+  if (workers < 1) workers = 1;
+  if (workers > 256) workers = 256;
+  ds_node **heads = (ds_node **)calloc(nbuckets, sizeof(ds_node *));
+  ds_job jobs[256];
+  pthread_t th[256];
+  *bad = 0;
+  double timed = 0;
+  const int ops[6] = {0, 1, 4, 2, 3, 5};
+  for (int k = 0; k < 6; ++k) {
+    const int op = ops[k];
+    const uint64_t items = (op == 4 || op == 5) ? nbuckets : n;
+    const double t0 = now_s();
+    for (int w = 0; w < workers; ++w) {
+      jobs[w].heads = heads;
+      jobs[w].nbuckets = nbuckets;
+      jobs[w].tseed = tseed;
+      jobs[w].kseed = kseed;
+      jobs[w].op = op;
+      jobs[w].bad = 0;
+      jobs[w].begin = items * (uint64_t)w / (uint64_t)workers;
+      jobs[w].end = items * (uint64_t)(w + 1) / (uint64_t)workers;
+      pthread_create(&th[w], NULL, ds_run, &jobs[w]);
+    }
+    for (int w = 0; w < workers; ++w) {
+      pthread_join(th[w], NULL);
+      *bad += jobs[w].bad;
+    }
+    if (k < 4) timed += now_s() - t0;
+  }
+  free(heads);
+  return timed;
+}
+
+typedef struct {
+  const uint32_t *lengths;
+  uint64_t begin, end, bad, pushes;
+  uint32_t start;
+} vec_job;
+
+static void *vec_run(void *arg) {
+  vec_job *j = (vec_job *)arg;
+  for (uint64_t v = j->begin; v < j->end; ++v) {
+    uint64_t cap = 1;
+    while (cap < j->start) cap <<= 1;
+    uint64_t size = 0;
+    uint32_t *data = (uint32_t *)malloc(cap * 4);
+    for (uint32_t i = 0; i < j->lengths[v] && data; ++i) {
+      if (size == cap) {
+        uint32_t *nd = (uint32_t *)malloc(cap * 8);
+        if (!nd) {
+          j->bad++;
+          break;
+        }
+        memcpy(nd, data, size * 4);
+        free(data);
+        data = nd;
+        cap *= 2;
+      }
+      data[size++] = (uint32_t)(v * 2654435761ull + i);
+      j->pushes++;
+    }
+    for (uint64_t i = 0; i < size; ++i) j->bad += data[i] != (uint32_t)(v * 2654435761ull + i);
+    free(data);
+  }
+  return NULL;
+}
+
+/* The vector-growth run with glibc; returns seconds. */
+double cpu_vectors(const uint32_t *lengths, uint64_t n, uint32_t start, int workers, uint64_t *bad,
+                   uint64_t *pushes) {
+  if (workers < 1) workers = 1;
+  if (workers > 256) workers = 256;
+  vec_job jobs[256];
+  pthread_t th[256];
+  const double t0 = now_s();
+  for (int w = 0; w < workers; ++w) {
+    jobs[w].lengths = lengths;
+    jobs[w].start = start;
+    jobs[w].bad = jobs[w].pushes = 0;
+    jobs[w].begin = n * (uint64_t)w / (uint64_t)workers;
+    jobs[w].end = n * (uint64_t)(w + 1) / (uint64_t)workers;
+    pthread_create(&th[w], NULL, vec_run, &jobs[w]);
+  }
+  *bad = *pushes = 0;
+  for (int w = 0; w < workers; ++w) {
+    pthread_join(th[w], NULL);
+    *bad += jobs[w].bad;
+    *pushes += jobs[w].pushes;
+  }
+  return now_s() - t0;
+}

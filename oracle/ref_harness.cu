@@ -16,6 +16,7 @@
 #include <stdio.h>
 
 #include "gallatin_gb300.h"  // gal_veb_op layout, op codes and serving structs only
+#include "ds_workloads.cuh"
 #include "serving.cuh"
 #include "workloads.cuh"
 
@@ -146,9 +147,57 @@ int launch_serving(void *dev, const galserve::server_t &sv, const galserve::trac
   return galserve::run((G *)dev, sv, t, p, o, 0, 4u * prop.multiProcessorCount, s) == cudaSuccess ? 0 : 2;
 }
 
+template <class G>
+int launch_table(void *dev, void *heads, uint64_t nbuckets, uint64_t seed, uint32_t op, const uint64_t *keys,
+                 uint64_t n, uint64_t key_seed, unsigned long long *stats, cudaStream_t s) {
+  galds::chaining_table<G> t;
+  t.alloc = (G *)dev;
+  t.heads = (typename galds::chaining_table<G>::block_type **)heads;
+  t.nbuckets = nbuckets;
+  t.seed = seed;
+  const uint64_t items = (op == 4 || op == 5) ? nbuckets : n;
+  if (items == 0) return 0;
+  galdswork::table_kernel<G><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(t, keys, n, key_seed, op, stats);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+template <class G>
+int launch_vectors(void *dev, const uint32_t *lengths, uint64_t n, uint32_t start, unsigned long long *stats,
+                   cudaStream_t s) {
+  if (n == 0) return 0;
+  galdswork::vectors_kernel<G><<<(unsigned)((n + 255) / 256), 256, 0, s>>>((G *)dev, lengths, n, start, stats);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
 }  // namespace
 
 extern "C" {
+
+// The same chained table and vectors (gallatin_gb300/structures.cuh) over the
+// reference allocator; heads is a zeroed device array of nbuckets pointers.
+int galref_table_op(void *h, void *heads, uint64_t nbuckets, uint64_t seed, uint32_t op, const uint64_t *d_keys,
+                    uint64_t n, uint64_t key_seed, unsigned long long *d_stats, void *stream) {
+  RefAlloc *a = (RefAlloc *)h;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a->config) {
+    case 0: return launch_table<ref_16m_16_4096>(a->dev, heads, nbuckets, seed, op, d_keys, n, key_seed, d_stats, s);
+    case 1: return launch_table<ref_16m_128_4096>(a->dev, heads, nbuckets, seed, op, d_keys, n, key_seed, d_stats, s);
+    case 2: return launch_table<ref_64m_16_4096>(a->dev, heads, nbuckets, seed, op, d_keys, n, key_seed, d_stats, s);
+    default: return launch_table<ref_4m_16_1024>(a->dev, heads, nbuckets, seed, op, d_keys, n, key_seed, d_stats, s);
+  }
+}
+
+int galref_run_vectors(void *h, const uint32_t *d_lengths, uint64_t n, uint32_t start, unsigned long long *d_stats,
+                       void *stream) {
+  RefAlloc *a = (RefAlloc *)h;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a->config) {
+    case 0: return launch_vectors<ref_16m_16_4096>(a->dev, d_lengths, n, start, d_stats, s);
+    case 1: return launch_vectors<ref_16m_128_4096>(a->dev, d_lengths, n, start, d_stats, s);
+    case 2: return launch_vectors<ref_64m_16_4096>(a->dev, d_lengths, n, start, d_stats, s);
+    default: return launch_vectors<ref_4m_16_1024>(a->dev, d_lengths, n, start, d_stats, s);
+  }
+}
 
 int galref_run_serving(void *h, const gal_serve_trace_t *tr, const gal_serve_params_t *pr, const gal_serve_out_t *out,
                        void *stream) {

@@ -52,3 +52,12 @@ def test_default_geometry_tiers():
     assert gal.classify(16 << 20) == ("block", 8, 1)
     assert gal.classify((16 << 20) + 1) == ("segment", 0, 2)
     assert gal.classify(256 << 20) == ("segment", 0, 16)
+
+
+def test_vector_lengths_shape():
+    from gallatin_gb300.workload import vector_lengths
+
+    v = vector_lengths()  # the benchmark's 1M vectors
+    assert v.dtype == np.uint32 and v.min() >= 1 and v.max() <= 65536
+    assert 60 <= int(np.median(v)) <= 68  # median 64
+    assert (v == 65536).sum() >= 1  # the cap is reached (sigma 1.5)
