@@ -200,7 +200,8 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   if ((rc = try_cuda(cudaMemset(s.chunk_ids, 0xFF, num_segments * sizeof(uint16_t)), "memset chunk_ids")) ||
       (rc = try_cuda(cudaMemset(s.seg_block_bits, 0, num_segments * s.seg_block_words * 8), "memset seg bits")) ||
       (rc = try_cuda(cudaMemset(s.block_meta, 0, nblocks * 8), "memset block_meta")) ||
-      (rc = try_cuda(cudaMemset(s.block_bits, 0, nblocks * 64 * 8), "memset block_bits")) ||
+      // every slice starts free; the bitmap is never rewritten afterwards
+      (rc = try_cuda(cudaMemset(s.block_bits, 0xFF, nblocks * 64 * 8), "memset block_bits")) ||
       (rc = try_cuda(cudaMemset(s.locks, 0, sizeof(uint32_t)), "memset locks")) ||
       (rc = try_cuda(cudaMemset(s.counters, 0, GAL_NUM_COUNTERS * 8), "memset counters")) ||
       (rc = try_cuda(cudaMemset(h->d_stats, 0, 64), "memset stats")))

@@ -345,8 +345,13 @@ __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
   }
 }
 
-__device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n) {
-  const uint64_t old = ptx::atom_add_release(st->block_meta + b, (uint64_t)(-(int64_t)n));
+// Give back n slices of block b's live count and act on the transitions.
+// `ordered`: the caller has already fenced (free_slice), so the add itself
+// can be relaxed.
+__device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n, bool ordered = false) {
+  const uint64_t delta = (uint64_t)(-(int64_t)n);
+  const uint64_t old =
+      ordered ? ptx::atom_add_relaxed(st->block_meta + b, delta) : ptx::atom_add_release(st->block_meta + b, delta);
   const uint32_t state = meta_state(old);
   const uint32_t live = meta_live(old);
   if ((state == GAL_STATE_DETACHED || state == GAL_STATE_WHOLE) && live == n) {
@@ -465,11 +470,14 @@ __device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint
 
 // ---- pinned blocks -------------------------------------------------------
 
+// The bitmap of a block that comes out of its segment is not rewritten: it
+// starts all ones at creation, slices only ever leave it by claims and come
+// back by frees, and a block-tier allocation leaves it alone, so the bitmap
+// of a FREE block is all ones once every free in flight has landed. A free
+// still in flight holds a 0 that nobody can claim until it turns to 1; that
+// is what lets free_slice return bits and live count in either order.
 __device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r) {
-  ulonglong2 *bits = reinterpret_cast<ulonglong2 *>(st->block_bits + (b << 6));
-  const ulonglong2 ones = make_ulonglong2(~0ull, ~0ull);
-  for (int i = 0; i < 32; ++i) bits[i] = ones;
-  own_block(st, b, t, r, GAL_STATE_PINNED, 0);  // release: bitmap before PINNED
+  own_block(st, b, t, r, GAL_STATE_PINNED, 0);
   count(st, GAL_CTR_BLOCK_PINS);
   count(st, GAL_CTR_TREE_PINS + (int)t);
 }
@@ -646,8 +654,13 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
         if (pick) {
           const uint64_t mask = expand_runs(pick, c);
           const uint64_t old = ptx::atom_and_acquire(bits + w, ~mask);
-          // a block serves one run length, so runs are taken or free whole
-          got = run_starts(old & mask, c) & pick;
+          const uint64_t gotbits = old & mask;
+          got = run_starts(gotbits, c) & pick;
+          // a run with a slice still on its way back (a free from the block's
+          // previous life, see pin_block) is not taken: return what of it
+          // this fetch-and cleared
+          const uint64_t partial = gotbits & ~expand_runs(got, c);
+          if (partial) ptx::red_or_relaxed(bits + w, partial);
           avail = old & ~mask;
         } else {
           avail = 0;
@@ -702,12 +715,16 @@ __device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t 
 
   const uint32_t wpeers = __match_any_sync(active, (unsigned long long)((b << 6) | word));
   const uint64_t or_mask = ptx::reduce_or64(wpeers, mask);
-  __syncwarp(active);  // every lane's payload writes before the release below
-  if (lane == (uint32_t)(__ffs((int)wpeers) - 1)) ptx::red_or_release(st->block_bits + (b << 6) + word, or_mask);
   const uint32_t bpeers = __match_any_sync(active, (unsigned long long)b);
   const uint32_t total = __reduce_add_sync(bpeers, c);
-  __syncwarp(active);  // bitmap returns before the live count drops
-  if (lane == (uint32_t)(__ffs((int)bpeers) - 1)) release_live(st, b, total);
+  // one fence orders every lane's payload writes before both returns: the
+  // next owner of these slices (through the bitmap) and the block's retire
+  // (through the live count) see them; the two returns need no order between
+  // them (see pin_block)
+  __syncwarp(active);
+  ptx::fence_acq_rel();
+  if (lane == (uint32_t)(__ffs((int)wpeers) - 1)) ptx::red_or_relaxed(st->block_bits + (b << 6) + word, or_mask);
+  if (lane == (uint32_t)(__ffs((int)bpeers) - 1)) release_live(st, b, total, true);
 }
 
 // ---- block and segment tiers ---------------------------------------------

@@ -53,6 +53,12 @@ __device__ __forceinline__ uint64_t atom_add_release(uint64_t *p, uint64_t v) {
   asm volatile("atom.release.gpu.global.add.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(v) : "memory");
   return r;
 }
+__device__ __forceinline__ uint64_t atom_add_relaxed(uint64_t *p, uint64_t v) {
+  uint64_t r;
+  asm volatile("atom.relaxed.gpu.global.add.u64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(v) : "memory");
+  return r;
+}
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ uint64_t atom_and_acquire(uint64_t *p, uint64_t v) {
   uint64_t r;
   asm volatile("atom.acquire.gpu.global.and.b64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(v) : "memory");
