@@ -40,6 +40,11 @@ sys.path.insert(0, str(REPO))
 GIB = 1 << 30
 MIB = 1 << 20
 REF_BATCH_PREFIX = 40
+# The reference allocator serves the serving trace's first 150 steps, but on
+# the full 600-step trace back-to-back runs exhaust its arena (blocks are
+# recycled only once every slice is back): by the fourth run every page
+# malloc returned NULL. Its arm, and a matching line of ours, use 150 steps.
+REF_SERVE_STEPS = 150
 
 WORKLOADS = {
     "mixed": dict(
@@ -99,7 +104,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"],
+                 "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
             )
         except OSError:
@@ -524,6 +529,8 @@ def run(args) -> dict | None:
 
         if args.serve_steps:
             w["steps"] = args.serve_steps
+        elif impl == "reference":
+            w["steps"] = REF_SERVE_STEPS
         trace = serving_trace(42, steps=w["steps"], arrivals_per_step=w["arrivals"])
         budget = int(w["gate"] * w["arena"]) // w["page_bytes"]
         srv_kw = dict(budget_pages=budget, page_bytes=w["page_bytes"], max_slots=w["slots"], max_pages=w["max_pages"])
@@ -715,6 +722,25 @@ def run(args) -> dict | None:
             plain["same_results"] = bool(np.array_equal(res0["checksum"], res["checksum"]) and
                                          np.array_equal(res0["admit_step"], res["admit_step"]))
             result["serving"]["plain_path"] = plain
+            # the device loop on the reference arm's sample (its first steps)
+            if w["steps"] != REF_SERVE_STEPS:
+                tr_s = serving_trace(42, steps=REF_SERVE_STEPS, arrivals_per_step=w["arrivals"])
+                srv_s = ServingRun(torch, tr_s, **srv_kw)
+                srv_s.run(a.run_serving, persistent=True, ctas_per_sm=geo, stream=s_ptr)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                flush.fill_(1)
+                e0.record(stream)
+                srv_s.run(a.run_serving, persistent=True, ctas_per_sm=geo, stream=s_ptr)
+                e1.record(stream)
+                e1.synchronize()
+                ms_s = e0.elapsed_time(e1)
+                short = summarize(srv_s.results(), page_bytes=w["page_bytes"], segment_bytes=w["segment"],
+                                  seconds=ms_s / 1e3)
+                short["ms_per_run"] = ms_s
+                short["sample"] = f"first {REF_SERVE_STEPS} steps (the reference arm's sample)"
+                result["serving"]["reference_sample"] = short
     if args.workload == "batches" and impl == "gb300":
         graph.close()
         if not args.no_prefix:
