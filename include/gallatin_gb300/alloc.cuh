@@ -50,6 +50,8 @@ constexpr int kAdoptCandidates = 64;
 // the slot cannot serve while another leader replaces its block
 constexpr uint32_t kNoMemBlock = 0xFFFFFFFEu;
 constexpr uint32_t kBusyBlock = 0xFFFFFFFDu;
+// leader-to-group flag on the cursor: the slices were taken by cursor alone
+constexpr uint32_t kFreshClaim = 1u << 31;
 
 // which detached blocks request_block may pin again
 enum { ADOPT_NONE = 0, ADOPT_ROOMY = 1, ADOPT_ANY = 2 };
@@ -362,16 +364,21 @@ __device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, 
 }
 
 // Move a block this thread owns from FREE to `state`, formatted for tree t
-// and run length 2^r, adding `live` to its live count.
+// and run length 2^r, adding `live` to its live count, with the cursor at 0
+// and the fresh flag as given. (A stale reservation may still add to live and
+// cursor meanwhile; its undo gives back live only, so it can only move the
+// cursor past positions that then stay free for a later pass.)
 __device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r,
-                                          uint32_t state, uint32_t live) {
+                                          uint32_t state, uint32_t live, bool fresh = false) {
   const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
   const int64_t dstate = (int64_t)state - (int64_t)meta_state(m);
   const int64_t dtree = (int64_t)t - (int64_t)meta_tree(m);
   const int64_t drun = (int64_t)r - (int64_t)meta_run(m);
+  const uint64_t dcursor = (uint64_t)(0x10000u - meta_cursor(m)) << GAL_META_CURSOR_SHIFT;  // wraps to 0
   const uint64_t delta = (uint64_t)(dstate * (1ll << GAL_META_STATE_SHIFT)) +
                          (uint64_t)(dtree * (1ll << GAL_META_TREE_SHIFT)) +
-                         (uint64_t)(drun * (1ll << GAL_META_RUN_SHIFT)) - (m & GAL_META_REUSED_BIT) + (uint64_t)live;
+                         (uint64_t)(drun * (1ll << GAL_META_RUN_SHIFT)) - (m & GAL_META_REUSED_BIT) -
+                         (m & GAL_META_FRESH_BIT) + (fresh ? GAL_META_FRESH_BIT : 0) + dcursor + (uint64_t)live;
   ptx::atom_add_release(st->block_meta + b, delta);
 }
 
@@ -407,7 +414,8 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
     for (int i = 0; i < 8; ++i) {
       if (!adopt_listed(m, k, roomy) || meta_live(m) + c > GAL_BLOCK_SLICES) break;
       const uint64_t nm =
-          (m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT)) | GAL_META_REUSED_BIT;
+          ((m - ((uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT)) | GAL_META_REUSED_BIT) &
+          ~GAL_META_FRESH_BIT;
       const uint64_t r = ptx::cas_acq_rel(st->block_meta + cand, m, nm);
       if (r == m) {
         adopt_sync_both(st, k, cand);
@@ -476,8 +484,16 @@ __device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint
 // of a FREE block is all ones once every free in flight has landed. A free
 // still in flight holds a 0 that nobody can claim until it turns to 1; that
 // is what lets free_slice return bits and live count in either order.
+// The block holds no slice here, so any 0 bit is such a free: with none, the
+// block is pinned fresh and its first pass hands out slices by cursor alone.
 __device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r) {
-  own_block(st, b, t, r, GAL_STATE_PINNED, 0);
+  const ulonglong2 *bits = reinterpret_cast<const ulonglong2 *>(st->block_bits + (b << 6));
+  uint64_t all = ~0ull;
+  for (int i = 0; i < 32; ++i) {
+    const ulonglong2 v = __ldcg(bits + i);
+    all &= v.x & v.y;
+  }
+  own_block(st, b, t, r, GAL_STATE_PINNED, 0, all == ~0ull);
   count(st, GAL_CTR_BLOCK_PINS);
   count(st, GAL_CTR_TREE_PINS + (int)t);
 }
@@ -610,10 +626,26 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
         }
         if (take > 0) {
           cursor = meta_cursor(m);
-          // a reused block's free slices are scattered: start leaders at
-          // hashed positions so they do not all chase the same word
-          if (m & GAL_META_REUSED_BIT) cursor *= 0x9E3779B1u;
-          cursor &= GAL_BLOCK_SLICES - 1;
+          const uint32_t span = take * c;
+          if ((m & GAL_META_FRESH_BIT) && cursor + span <= GAL_BLOCK_SLICES) {
+            // first pass of a fresh block: [cursor, cursor + span) is free
+            // and ours; clear those bits without waiting for the answer
+            uint64_t *const fbits = st->block_bits + ((uint64_t)b << 6);
+            for (uint32_t pos = cursor; pos < cursor + span;) {
+              const uint32_t lo = pos & 63;
+              const uint32_t n = 64 - lo < cursor + span - pos ? 64 - lo : cursor + span - pos;
+              ptx::red_and_relaxed(fbits + (pos >> 6), ~((n >= 64 ? ~0ull : ((1ull << n) - 1)) << lo));
+              pos += n;
+            }
+            cursor |= kFreshClaim;
+          } else {
+            // past the first pass: the cursor must not look fresh after it wraps
+            if (m & GAL_META_FRESH_BIT) ptx::red_and_relaxed(st->block_meta + b, ~GAL_META_FRESH_BIT);
+            // a reused block's free slices are scattered: start leaders at
+            // hashed positions so they do not all chase the same word
+            if (m & GAL_META_REUSED_BIT) cursor *= 0x9E3779B1u;
+            cursor &= GAL_BLOCK_SLICES - 1;
+          }
         } else {
           b = GAL_EMPTY_BLOCK;
         }
@@ -628,6 +660,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
       }
     }
     b = __shfl_sync(grp, b, leader);
+    cursor = __shfl_sync(grp, cursor, leader);
     if (b == kNoMemBlock) {
       if (++strikes >= nslots) done = true;  // every slot tried: the arena cannot serve this class now
       continue;
@@ -638,6 +671,19 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     }
     if (b == GAL_EMPTY_BLOCK) continue;
     take = __shfl_sync(grp, take, leader);
+    if (cursor & kFreshClaim) {  // the leader already holds these slices
+      if (g_rank < take) {
+        const uint64_t slice = (cursor & ~kFreshClaim) + g_rank * c;
+        result = block_address(st, b, t) + (slice << (st->min_shift + (int)t));
+        done = true;
+      }
+      if (refill && lane == (uint32_t)leader) {
+        count(st, GAL_CTR_REPLACE_REFILL);
+        uint32_t nb;
+        replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ROOMY, &nb);  // no nearly-full blocks
+      }
+      continue;
+    }
 
     uint64_t *const bits = st->block_bits + ((uint64_t)b << 6);
     int my_slice = -1;

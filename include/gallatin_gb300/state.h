@@ -52,6 +52,9 @@
  *   bits 42-45  log2 of the run length the block serves (largest tree only)
  *   bit  46     reused: pinned again while it still held slices, so its free
  *               slices are scattered and the cursor does not point at them
+ *   bit  47     fresh: pinned from its segment with every bitmap bit set and
+ *               the cursor at 0; while the cursor has not passed 4096 the
+ *               reserved positions are exactly the free slices
  *   bits 48-63  cursor: position hint for the next claim, wraps mod 2^16
  * All transitions are atomic adds of field deltas (or a CAS for the
  * conditional retire) so concurrent reservations and their undos commute. */
@@ -60,6 +63,7 @@
 #define GAL_META_STATE_SHIFT 40
 #define GAL_META_RUN_SHIFT 42
 #define GAL_META_REUSED_BIT (1ull << 46)
+#define GAL_META_FRESH_BIT (1ull << 47)
 #define GAL_META_CURSOR_SHIFT 48
 #define GAL_STATE_FREE 0u
 #define GAL_STATE_PINNED 1u
