@@ -20,6 +20,14 @@ struct gal_device_alloc {
     for (uint64_t w = 0; w < t.layer_words[t.num_layers - 1]; ++w) free_segments += __popcll(__ldcg(leaf + w));
     return state.num_segments - free_segments;
   }
+  // the same, counted by the 32 lanes of a converged warp (all lanes get it)
+  __device__ inline uint64_t owned_segments_warp(uint32_t lane) const {
+    const gal_veb_t &t = state.segment_tree;
+    const unsigned long long *leaf = (const unsigned long long *)t.bits[t.num_layers - 1];
+    uint32_t free_segments = 0;
+    for (uint64_t w = lane; w < t.layer_words[t.num_layers - 1]; w += 32) free_segments += __popcll(__ldcg(leaf + w));
+    return state.num_segments - __reduce_add_sync(0xffffffffu, free_segments);
+  }
 };
 
 #endif  // GALLATIN_GB300_DEVICE_ALLOC_CUH

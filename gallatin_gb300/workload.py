@@ -206,14 +206,16 @@ def single_stream(trace: dict, i: int, extra_steps: int = 2) -> dict:
             "ids": np.array([i], dtype=np.uint32)}
 
 
-def serving_admission(trace: dict, budget_pages: int, max_slots: int):
+def serving_admission(trace: dict, budget_pages: int, max_slots: int, slot_delay: int = 1):
     """Host model of the serving loop's first-come-first-served admission (the
     device loop must reproduce it exactly). At step s, k_s streams are
     admitted: the largest k such that they have arrived by step s, k free slots
     exist, and the pages committed to admitted, unfinished streams plus their
     pages stay within budget_pages. Every admitted stream takes one page per
-    step; a stream with p pages admitted at step a finishes at step a + p - 1,
-    and its slot and pages count as free for the admission of step a + p.
+    step; a stream with p pages admitted at step a finishes at step a + p - 1;
+    its pages count as free for the admission of step a + p and its slot, which
+    the loop reuses only after the stream's pages are freed in step a + p, for
+    step a + p + slot_delay.
 
     Returns (admit_step u32[n], 0xFFFFFFFF = never admitted within the steps;
     per-step arrays: admitted, committed pages after the step's admissions)."""
@@ -245,7 +247,7 @@ def serving_admission(trace: dict, budget_pages: int, max_slots: int):
             free_slots -= k
             fin = s + p
             np.add.at(release_pages, np.minimum(fin, steps + 1), p)
-            np.add.at(release_slots, np.minimum(fin, steps + 1), 1)
+            np.add.at(release_slots, np.minimum(fin + slot_delay, steps + 1), 1)
             nxt += k
         out_k[s] = k
         out_committed[s] = committed

@@ -206,12 +206,15 @@ int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_
  * Admission is first-come first-served on the device: at step s the longest
  * run of waiting streams is admitted that has arrived (arrivals_end[s + 1]),
  * fits the free slots (max_slots), and keeps the pages committed to admitted,
- * unfinished streams within budget_pages. A stream finishing at step s frees
- * its slot and pages for the admission of step s + 1. After the last step the
- * unfinished streams' pages are freed, so the allocator ends as it started.
+ * unfinished streams within budget_pages. A stream finishing at step s gives
+ * back its pages for the admission of step s + 1; its pages are read back and
+ * freed during step s + 1 (overlapping that step's mallocs) and its slot
+ * counts as free for the admission of step s + 2. After the last step every
+ * page still held is freed, so the allocator ends as it started.
  * mode 0: the plain path, one launch per phase per step (phase 1: a thread
- * per stream takes its page; phase 2: finished streams return theirs);
- * mode 1: every step in one cooperative persistent launch. */
+ * per stream takes its page, and finished streams' pages are freed; phase 2:
+ * slots return and admission); mode 1: every step in one cooperative
+ * persistent launch. */
 typedef struct gal_serve_trace_t {
   uint32_t n_streams;
   uint32_t pad_;

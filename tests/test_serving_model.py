@@ -47,7 +47,10 @@ def test_admission_model_keeps_its_rules():
     for s in range(tr["steps"]):
         running = adm & (admit <= s) & (admit.astype(np.int64) + pages - 1 >= s)
         assert pages[running].sum() <= budget
-        assert running.sum() <= slots
+        # a slot stays taken one step past its stream's last page (its pages
+        # are freed in that step)
+        holding = adm & (admit <= s) & (admit.astype(np.int64) + pages >= s)
+        assert holding.sum() <= slots
         assert st["committed"][s] == pages[running].sum()
     # the budget binds at some step (the gate is exercised)
     assert st["committed"].max() > 0.9 * budget
