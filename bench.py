@@ -322,6 +322,13 @@ def run(args) -> dict | None:
         w["arena"] = int(args.arena_gib * GIB)
     if args.batches and "batches" in w:
         w["batches"] = args.batches
+    if args.serve_slots and "slots" in w:
+        w["slots"] = args.serve_slots
+    if args.keys and "keys" in w:
+        w["keys"] = args.keys
+        w["buckets"] = max(args.keys // 4, 1)
+    if args.vectors and "vectors" in w:
+        w["vectors"] = args.vectors
     if args.batch_hi and "batches" in w:
         w["batch_hi"] = args.batch_hi
     impl = args.impl
@@ -797,6 +804,9 @@ def main() -> int:
     ap.add_argument("--no-prefix", action="store_true",
                     help="batches: skip the timing on the reference's sample; serving: skip the plain-path run")
     ap.add_argument("--serve-steps", type=int, default=0, help="override the serving workload's step count")
+    ap.add_argument("--serve-slots", type=int, default=0, help="override the serving loop's stream slots")
+    ap.add_argument("--keys", type=int, default=0, help="override the table workload's key count (buckets = keys / 4)")
+    ap.add_argument("--vectors", type=int, default=0, help="override the vector count")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     res = run(args)
