@@ -153,14 +153,21 @@ def dist_setup():
     return world, rank, local
 
 
-def barrier_max(torch, world: int, value: float) -> float:
+def barrier_max(torch, world: int, value: float, device: str = "cuda") -> float:
+    """The largest of every rank's value (the slowest replica's time)."""
     if world == 1:
         return value
     import torch.distributed as dist
 
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units: int, steps: int, world: int, slowest_total_ms: float) -> float:
+    """Whole-job throughput of `world` independent replicas that each process
+    `units` per step: every replica's work over the slowest replica's time."""
+    return units * steps * world / (slowest_total_ms / 1e3)
 
 
 def barrier(torch, world: int):
@@ -306,13 +313,18 @@ def run(args) -> dict | None:
     import torch
 
     world, rank, local = dist_setup()
+    if args.impl == "reference" and world > 1:
+        # the reference arm runs once, on rank 0's GPU; the other ranks exit
+        if rank != 0:
+            return None
+        world = 1
     if world > 1:
         import torch.distributed as dist
 
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     else:
-        torch.cuda.set_device(0)
+        torch.cuda.set_device(local)
     w = dict(WORKLOADS[args.workload])
     if args.threads:
         w["threads"] = args.threads
@@ -614,7 +626,7 @@ def run(args) -> dict | None:
     st = stats.cpu().numpy()
     total_ms = barrier_max(torch, world, float(sum(times)))
     ms_per_step = total_ms / args.steps
-    value = units * args.steps * world / (total_ms / 1e3)
+    value = replica_throughput(units, args.steps, world, total_ms)
 
     e2e = None
     if e2e_step is not None and not args.no_e2e:
@@ -632,7 +644,7 @@ def run(args) -> dict | None:
             e2e_bad += out
         e2e_total = barrier_max(torch, world, float(sum(e2e_times)))
         e2e = {
-            "value": units * args.steps * world / e2e_total,
+            "value": replica_throughput(units, args.steps, world, e2e_total * 1e3),
             "unit": unit,
             "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h if args.workload == "serving" else 64,

@@ -90,7 +90,7 @@ enum gal_counter_id {
   GAL_CTR_BLOCK_RETIRE = 9,
   GAL_CTR_REPLACE_EMPTY = 10, /* slot had no block yet */
   GAL_CTR_REPLACE_FULL = 11,  /* pinned block had no room left */
-  GAL_CTR_REPLACE_FRAG = 12,  /* no aligned run for a multi-slice request */
+  GAL_CTR_REPLACE_FRAG = 12,  /* unused: blocks serve one run length, so runs do not fragment */
   GAL_CTR_CLAIM_SHORT = 13,   /* reservation held but bits not found in time */
   GAL_CTR_STALE_SLOT = 14,    /* slot changed between read and reservation */
   GAL_CTR_SLOT_BUSY = 15,     /* slot was being replaced */
