@@ -9,6 +9,8 @@ verifies and frees; plus 256 segment-tier requests of 16-256 MiB (thread 0
 of every 64th 256-thread CTA). One step = one launch of that workload kernel.
 `--workload pairs` runs the small plain configuration instead: a 2 GiB arena,
 1,048,576 threads (1024 x 1024), malloc 16 B / store tid / verify / free.
+The other workloads (batches, table, vectors, serving, spill, calloc) are
+described where WORKLOADS defines them.
 
 value: pairs/s with the class trace resident in HBM, device time from CUDA
 events on the launching stream, L2 flushed (256 MiB write) before every
@@ -73,6 +75,19 @@ WORKLOADS = {
     "mixed-slices": dict(
         arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=4_194_304, rounds=8, block=256,
         seg_every=0, seg_lo=16 * MIB, seg_hi=256 * MIB,
+    ),
+    # device first, host arena when the device arena is out of room (the
+    # reference's global_malloc_fused / global_free_fused): 8,388,608
+    # allocations of 16..4096 B (about 7.6 GB) against a 4 GiB device arena
+    # and an 8 GiB pinned host arena; one step = a fill launch (malloc, write
+    # the first and last u64) and a drain launch (verify, free)
+    "spill": dict(arena=4 * GIB, host_arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096,
+                  threads=8_388_608),
+    # the mixed-slices workload on an allocator that returns zeroed memory
+    # (the reference's running_calloc): every free zeroes its slices
+    "calloc": dict(
+        arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=4_194_304, rounds=8, block=256,
+        seg_every=0, seg_lo=16 * MIB, seg_hi=256 * MIB, calloc=True,
     ),
 }
 
@@ -177,16 +192,20 @@ def barrier(torch, world: int):
         dist.barrier()
 
 
-def make_allocator(impl: str, w: dict):
+def make_allocator(impl: str, w: dict, host: bool = False):
+    """The workload's allocator; host=True: the second one, over pinned host
+    memory (w["host_arena"] bytes), for the spill workload."""
+    size = w["host_arena"] if host else w["arena"]
+    seed = 43 if host else 42
     if impl == "reference":
         import oracle
 
-        return oracle.RefGallatin(w["arena"], 42, w["segment"], w["min_size"], w["max_size"])
+        return oracle.RefGallatin(size, seed, w["segment"], w["min_size"], w["max_size"], host_arena=host)
     import gallatin_gb300 as gal
 
-    return gal.Gallatin.generate_on_device(
-        w["arena"], 42, print_info=False, segment_size=w["segment"], min_size=w["min_size"], max_size=w["max_size"]
-    )
+    make = gal.Gallatin.generate_on_device_host if host else gal.Gallatin.generate_on_device
+    return make(size, seed, print_info=False, running_calloc=bool(w.get("calloc")), segment_size=w["segment"],
+                min_size=w["min_size"], max_size=w["max_size"])
 
 
 def close_allocator(impl: str, a) -> None:
@@ -201,6 +220,22 @@ def cpu_baseline(name: str, w: dict) -> dict:
     import oracle
 
     cores = os.cpu_count() or 1
+    if name == "calloc":
+        n, rounds = w["threads"], w["rounds"]
+        secs, misses, bad = oracle.cpu_replay_mixed_zeroed(n, 0, n, rounds, 42, workers=cores)
+        return {"value": n * rounds / secs, "unit": "malloc+free pairs/s", "cores": cores, "kind": "port",
+                "seconds": secs, "misses": misses, "verify_failures": bad,
+                "sample": f"full workload: {n} threads x {rounds} rounds through glibc calloc (each allocation "
+                          "checked to read zero), fill, verify, free"}
+    if name == "spill":
+        from gallatin_gb300.workload import mixed_class_trace
+
+        classes = mixed_class_trace(w["threads"], 1, 42).reshape(-1)
+        secs, misses, bad = oracle.cpu_replay_fill_drain(classes, cores)
+        return {"value": len(classes) / secs, "unit": "malloc+free pairs/s", "cores": cores, "kind": "port",
+                "seconds": secs, "misses": misses, "verify_failures": bad,
+                "sample": f"full workload: {len(classes)} glibc mallocs (fill), then verify and free (drain); host "
+                          "memory has no device arena to spill from"}
     if name in ("mixed", "mixed-slices"):
         n, rounds = w["threads"], w["rounds"]
         secs, misses, bad = oracle.cpu_replay_mixed(
@@ -362,6 +397,16 @@ def run(args) -> dict | None:
                                    "traps in set_tree_id, gallatin.cuh:1477-1489); not run again",
                 }))
             return None
+        if args.workload == "calloc":
+            if rank == 0:
+                print(json.dumps({
+                    "impl": "reference",
+                    "unavailable": "the reference's running_calloc needs dynamic parallelism with relocatable device "
+                                   "code (gallatin.cuh:1306-1369) and its block clear returns blocks without zeroing "
+                                   "them (memory_table.cuh:101-136), so it is not a zeroed-memory allocator to "
+                                   "compare with",
+                }))
+            return None
         if oracle.load_ref() is None:
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "reference CUDA build (oracle/_ref) is not built"}))
@@ -376,10 +421,51 @@ def run(args) -> dict | None:
     stream = torch.cuda.current_stream()
     s_ptr = stream.cuda_stream
     a = make_allocator(impl, w)
+    ha = None
+    if args.workload == "spill":
+        try:
+            ha = make_allocator(impl, w, host=True)
+        except RuntimeError as e:
+            close_allocator(impl, a)
+            if rank == 0:
+                print(json.dumps({"impl": impl, "unavailable": f"host-arena allocator: {e}"}))
+            return None
+    launches_per_step = 1
     stats = torch.zeros(8, dtype=torch.int64, device="cuda")
     flush = torch.empty(256 * MIB, dtype=torch.uint8, device="cuda")
 
-    if args.workload in ("mixed", "mixed-slices"):
+    if args.workload == "spill":
+        from gallatin_gb300.workload import mixed_class_trace
+
+        n = w["threads"]
+        trace = mixed_class_trace(n, 1, 42).reshape(-1)
+        d_trace = torch.from_numpy(trace).cuda()
+        h_trace = torch.from_numpy(trace).pin_memory()
+        d_table = torch.zeros(n, dtype=torch.int64, device="cuda")
+        units = n
+        # 8 B pointer record written and read back, 16 B payload written and
+        # 16 B read back per allocation
+        alg_bytes = n * 48
+        launches_per_step = 2
+
+        def step():
+            a.run_fused(ha, n, 42, d_table.data_ptr(), stats.data_ptr(), d_classes=d_trace.data_ptr(), phases=3,
+                        stream=s_ptr)
+
+        e2e_step = None
+        if impl == "gb300":
+            def e2e_step():
+                return a.run_fused_host(ha, n, 42, h_trace.data_ptr(), stream=s_ptr)
+
+        h2d = n
+        config = {
+            "workload": "device-first malloc with a pinned host-arena fallback (fused): fill n allocations of "
+                        "16..4096 B powers of two, then verify and free each",
+            "arena_bytes": w["arena"], "host_arena_bytes": w["host_arena"], "segment_bytes": w["segment"],
+            "min_size": w["min_size"], "max_size": w["max_size"], "allocations": n, "seed": 42,
+            "l2": "flushed (256 MiB write) before every timed step",
+        }
+    elif args.workload in ("mixed", "mixed-slices", "calloc"):
         from gallatin_gb300.workload import mixed_class_trace, mixed_mean_bytes
 
         n, rounds = w["threads"], w["rounds"]
@@ -399,8 +485,11 @@ def run(args) -> dict | None:
                                     seg_lo=w["seg_lo"], seg_hi=w["seg_hi"], block_dim=w["block"], stream=s_ptr)
 
         h2d = n * rounds
+        if args.workload == "calloc":
+            alg_bytes += n * rounds * mixed_mean_bytes()  # the zeroing write of every free
         config = {
-            "workload": "mixed sizes 16..4096 B powers of two, 8 rounds malloc/fill/verify/free",
+            "workload": "mixed sizes 16..4096 B powers of two, 8 rounds malloc/fill/verify/free" + (
+                ", zeroed on free (calloc)" if args.workload == "calloc" else ""),
             "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
             "max_size": w["max_size"], "threads": n, "rounds": rounds, "block_dim": w["block"],
             "segment_tier_requests": seg_requests, "segment_tier_bytes": [w["seg_lo"], w["seg_hi"]], "seed": 42,
@@ -695,7 +784,7 @@ def run(args) -> dict | None:
         "roofline": roofline,
         "e2e": e2e,
         "clocks": clocks.summary(),
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_step,
         "misses": int(st[0]),
         "verify_failures": int(st[1]),
         "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
@@ -770,6 +859,9 @@ def run(args) -> dict | None:
             close_allocator(impl, a)
             a = None
             result_autotune = autotune_batches(reqs, offsets, slots, arena=w["arena"])
+    if args.workload == "spill":
+        result["spill"] = {"host_served": int(st[4]), "host_fraction": int(st[4]) / max(units * args.steps, 1)}
+        close_allocator(impl, ha)
     if impl == "gb300" and a is not None:
         st_all = a.stats()
         result["allocator_counters"] = st_all["counters"]

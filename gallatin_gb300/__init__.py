@@ -6,8 +6,9 @@ libgallatin_gb300.so (include/gallatin_gb300.h) builds, inspects and destroys
 allocator state and runs batch kernels over it. This module binds that
 library with ctypes and mirrors the reference's host interface
 (gallatin::allocators::Gallatin<seg, min, max>::generate_on_device /
-free_on_device / print_info, and init_global_allocator / free_global_allocator
-/ print_global_stats from global_allocator.cuh:48-97).
+generate_on_device_host / free_on_device / print_info, and the global
+allocator functions of global_allocator.cuh:41-216: init_global_allocator /
+free_global_allocator / print_global_stats, their _host and _combined forms).
 
 Device buffers are passed as integer device addresses and streams as integer
 cudaStream_t handles, so any CUDA buffer provider works (the tests use torch).
@@ -34,6 +35,14 @@ __all__ = [
     "free_global_allocator",
     "print_global_stats",
     "global_allocator",
+    "init_global_allocator_host",
+    "free_global_allocator_host",
+    "print_global_stats_host",
+    "global_host_allocator",
+    "init_global_allocator_combined",
+    "free_global_allocator_combined",
+    "FLAG_HOST_ARENA",
+    "FLAG_CALLOC",
     "OPS",
     "DUMP",
     "COUNTERS",
@@ -46,6 +55,8 @@ GAL_EMPTY_BLOCK = 0xFFFFFFFF
 GAL_FREE_SEGMENT = 0xFFFF
 GAL_SEG_GATE = -(1 << 28)
 NOALLOC_TRACE_MAX_BYTES = 2 << 20
+FLAG_HOST_ARENA = 1  # arena in pinned host memory mapped into the GPU
+FLAG_CALLOC = 2  # malloc returns zeroed bytes (zero on free)
 
 OPS = {
     "insert": 0,
@@ -129,7 +140,7 @@ class _Geometry(ctypes.Structure):
         ("total_slots", c_uint32),
         ("slot_count", c_uint32 * GAL_MAX_TREES),
         ("num_classes", c_uint32),
-        ("pad_", c_uint32),
+        ("flags", c_uint32),
         ("arena_base", c_uint64),
     ]
 
@@ -170,6 +181,7 @@ def load(path: str | Path | None = None):
     vp, u64, u32, i32 = c_void_p, c_uint64, c_uint32, c_int
     sigs = {
         "gal_create": (i32, [u64, u64, u64, u64, u64, u32, POINTER(vp)]),
+        "gal_create_ex": (i32, [u64, u64, u64, u64, u64, u32, u32, POINTER(vp)]),
         "gal_destroy": (i32, [vp]),
         "gal_device_state": (vp, [vp]),
         "gal_from_device_state": (vp, [vp]),
@@ -187,6 +199,9 @@ def load(path: str | Path | None = None):
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host_noalloc": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
+        "gal_run_fused": (i32, [vp, vp, u64, u64, vp, vp, u32, vp, vp]),
+        "gal_run_fused_host": (i32, [vp, vp, u64, u64, vp, vp, vp]),
+        "gal_run_zeroed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, vp]),
         "gal_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, u32, vp, vp]),
         "gal_capture_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, u32, u32, vp, POINTER(vp)]),
         "gal_graph_launch": (i32, [vp, vp]),
@@ -266,6 +281,9 @@ class Gallatin:
         self.num_classes = g.num_classes
         self.slot_count = list(g.slot_count)[: g.num_classes]
         self.arena_base = g.arena_base
+        self.flags = g.flags
+        self.host_arena = bool(g.flags & FLAG_HOST_ARENA)
+        self.calloc = bool(g.flags & FLAG_CALLOC)
 
     @classmethod
     def generate_on_device(
@@ -280,16 +298,47 @@ class Gallatin:
         max_size: int = 4096,
         min_slots: int = 0,
     ) -> "Gallatin":
-        del running_calloc  # calloc via dynamic parallelism is not provided
+        """running_calloc: every malloc returns zeroed bytes (zero on free)."""
+        return cls._generate(max_bytes, seed, print_info, FLAG_CALLOC if running_calloc else 0, segment_size,
+                             min_size, max_size, min_slots)
+
+    @classmethod
+    def generate_on_device_host(
+        cls,
+        max_bytes: int,
+        seed: int,
+        print_info: bool = True,
+        running_calloc: bool = False,
+        *,
+        segment_size: int = 16 << 20,
+        min_size: int = 16,
+        max_size: int = 4096,
+        min_slots: int = 0,
+    ) -> "Gallatin":
+        """The allocator over pinned host memory mapped into the GPU
+        (reference generate_on_device_host, gallatin.cuh:423-526): the arena
+        is host memory, the metadata stays on the device."""
+        flags = FLAG_HOST_ARENA | (FLAG_CALLOC if running_calloc else 0)
+        return cls._generate(max_bytes, seed, print_info, flags, segment_size, min_size, max_size, min_slots)
+
+    @classmethod
+    def _generate(cls, max_bytes, seed, print_info, flags, segment_size, min_size, max_size, min_slots):
         h = c_void_p()
-        _check(load().gal_create(max_bytes, seed, segment_size, min_size, max_size, min_slots, ctypes.byref(h)))
+        _check(load().gal_create_ex(max_bytes, seed, segment_size, min_size, max_size, min_slots, flags,
+                                    ctypes.byref(h)))
         obj = cls(h.value, segment_size, min_size, max_size)
         if print_info:
+            where = "pinned host" if flags & FLAG_HOST_ARENA else "device"
             print(
                 f"Booted Gallatin with {obj.num_trees} trees in range {min_size}-{max_size} and "
-                f"{max_bytes / 2**30:f} GB of memory {obj.num_segments} segments"
+                f"{max_bytes / 2**30:f} GB of {where} memory {obj.num_segments} segments"
             )
         return obj
+
+    def owns_allocation(self, ptr: int) -> bool:
+        """Whether a pointer lies in this allocator's arena (reference
+        owns_allocation, gallatin.cuh:2027, memory_table.cuh:1346)."""
+        return 0 <= ptr - self.arena_base < self.arena_bytes
 
     def free_on_device(self) -> None:
         if self._h:
@@ -411,6 +460,30 @@ class Gallatin:
             )
         )
         return out
+
+    # -- device first, host arena fallback ------------------------------------
+    def run_fused(self, host: "Gallatin | None", n: int, seed: int, d_table: int, d_stats: int, *,
+                  d_classes: int = 0, phases: int = 3, stream: int = 0) -> None:
+        """Fill/drain of n allocations through the fused calls (see
+        gal_run_fused): this allocator first, `host` when it returns NULL.
+        phases: 1 fill, 2 drain, 3 both."""
+        _check(load().gal_run_fused(self.handle, host.handle if host is not None else None, n, seed, d_classes,
+                                    d_table, phases, d_stats, stream))
+
+    def run_fused_host(self, host: "Gallatin | None", n: int, seed: int, h_classes_ptr: int,
+                       stream: int = 0) -> np.ndarray:
+        """Both phases end to end from a host class trace; returns the 8 stats words."""
+        out = np.zeros(8, dtype=np.uint64)
+        _check(load().gal_run_fused_host(self.handle, host.handle if host is not None else None, n, seed,
+                                         h_classes_ptr, out.ctypes.data, stream))
+        return out
+
+    def run_zeroed(self, n_threads: int, rounds: int, seed: int, d_stats: int, *, big_every: int = 0,
+                   big_lo: int = 64 << 10, big_hi: int = 1 << 20, stream: int = 0) -> None:
+        """Zeroed-memory check (see gal_run_zeroed): stats[1] counts
+        allocations that held a non-zero byte."""
+        _check(load().gal_run_zeroed(self.handle, n_threads, rounds, seed, big_every, big_lo, big_hi, d_stats,
+                                     stream))
 
     # -- batched request streams ---------------------------------------------
     def run_batches(self, d_reqs: int, d_offsets: int, offsets: np.ndarray, d_table: int, d_stats: int, *,
@@ -627,3 +700,46 @@ def free_global_allocator() -> None:
 
 def print_global_stats() -> None:
     global_allocator().print_info()
+
+
+# -- host-memory and combined global allocators (global_allocator.cuh:98-183) --
+_GLOBAL_HOST: Gallatin | None = None
+
+
+def init_global_allocator_host(num_bytes: int, seed: int, print_info: bool = True,
+                               running_calloc: bool = False) -> Gallatin:
+    """Create the process-wide Gallatin<16 MiB, 16, 4096> over pinned host memory."""
+    global _GLOBAL_HOST
+    if _GLOBAL_HOST is not None:
+        _GLOBAL_HOST.free_on_device()
+    _GLOBAL_HOST = Gallatin.generate_on_device_host(num_bytes, seed, print_info, running_calloc)
+    return _GLOBAL_HOST
+
+
+def global_host_allocator() -> Gallatin:
+    if _GLOBAL_HOST is None:
+        raise GalError("init_global_allocator_host has not been called")
+    return _GLOBAL_HOST
+
+
+def free_global_allocator_host() -> None:
+    global _GLOBAL_HOST
+    if _GLOBAL_HOST is not None:
+        _GLOBAL_HOST.free_on_device()
+        _GLOBAL_HOST = None
+
+
+def print_global_stats_host() -> None:
+    global_host_allocator().print_info()
+
+
+def init_global_allocator_combined(num_bytes: int, host_bytes: int, seed: int, print_info: bool = True,
+                                   running_calloc: bool = False) -> tuple[Gallatin, Gallatin]:
+    """Both the device and the host-memory global allocators."""
+    return (init_global_allocator(num_bytes, seed, print_info, running_calloc),
+            init_global_allocator_host(host_bytes, seed, print_info, running_calloc))
+
+
+def free_global_allocator_combined() -> None:
+    free_global_allocator()
+    free_global_allocator_host()

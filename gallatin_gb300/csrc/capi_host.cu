@@ -98,8 +98,14 @@ extern "C" const char *gal_last_error(void) { return g_last_error; }
 
 extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size,
                           uint64_t max_size, uint32_t min_slots, gal_allocator **out) {
+  return gal_create_ex(max_bytes, seed, segment_bytes, min_size, max_size, min_slots, 0, out);
+}
+
+extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size,
+                             uint64_t max_size, uint32_t min_slots, uint32_t flags, gal_allocator **out) {
   if (out == nullptr) return fail_invalid("out is NULL");
   *out = nullptr;
+  if (flags & ~(GAL_FLAG_HOST_ARENA | GAL_FLAG_CALLOC)) return fail_invalid("unknown flags");
   if (!is_pow2(segment_bytes) || !is_pow2(min_size) || !is_pow2(max_size))
     return fail_invalid("segment, min and max sizes must be powers of two");
   if (max_size < min_size) return fail_invalid("max_size < min_size");
@@ -132,6 +138,9 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   h->d_bsorted_bytes = h->d_bbins_bytes = 0;
   h->d_serve = nullptr;
   h->d_serve_bytes = 0;
+  h->d_ftable = nullptr;
+  h->d_ftable_bytes = 0;
+  h->host_arena = nullptr;
   h->min_size = min_size;
   h->max_size = max_size;
   gal_state_t &s = h->hs;
@@ -152,6 +161,7 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   s.num_classes = (uint32_t)(num_trees + max_run);
   s.num_sms = (uint32_t)prop.multiProcessorCount;
   s.seed = seed;
+  s.flags = flags;
   // Pinned blocks per slot class: one per SM for small trees; for large
   // trees as many as a quarter of the arena split evenly over the trees
   // affords (a block of tree t is 4096 slices of min << t bytes). A run
@@ -178,10 +188,30 @@ extern "C" int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_by
   int rc = GAL_OK;
   auto cleanup = [&](int code) {
     free_all(h->device_allocs);
+    if (h->host_arena) cudaFreeHost(h->host_arena);
     delete h;
     return code;
   };
-  if ((rc = device_alloc(h, &s.memory, s.arena_bytes, "cudaMalloc arena")) != GAL_OK) return cleanup(rc);
+  if (flags & GAL_FLAG_HOST_ARENA) {
+    // pinned host pages mapped into the GPU's address space (the reference's
+    // host_only table, memory_table.cuh:521-540); with unified addressing the
+    // device address equals the host address
+    if (!prop.canMapHostMemory) return cleanup(fail_invalid("device cannot map host memory"));
+    cudaError_t e = cudaHostAlloc((void **)&h->host_arena, s.arena_bytes, cudaHostAllocMapped);
+    if (e != cudaSuccess) {
+      h->host_arena = nullptr;
+      return cleanup(galcapi::fail_cuda(e, "cudaHostAlloc arena"));
+    }
+    e = cudaHostGetDevicePointer((void **)&s.memory, h->host_arena, 0);
+    if (e != cudaSuccess) return cleanup(galcapi::fail_cuda(e, "cudaHostGetDevicePointer arena"));
+    if (flags & GAL_FLAG_CALLOC) memset(h->host_arena, 0, s.arena_bytes);
+  } else {
+    if ((rc = device_alloc(h, &s.memory, s.arena_bytes, "cudaMalloc arena")) != GAL_OK) return cleanup(rc);
+    if (flags & GAL_FLAG_CALLOC) {
+      const cudaError_t e = cudaMemset(s.memory, 0, s.arena_bytes);
+      if (e != cudaSuccess) return cleanup(galcapi::fail_cuda(e, "memset arena"));
+    }
+  }
   if ((rc = device_alloc(h, &s.chunk_ids, num_segments, "cudaMalloc chunk_ids")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.seg_avail, num_segments, "cudaMalloc seg_avail")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.seg_block_bits, num_segments * s.seg_block_words, "cudaMalloc seg bits")) != GAL_OK)
@@ -255,7 +285,9 @@ extern "C" int gal_destroy(gal_allocator *h) {
   if (h->d_bsorted) cudaFree(h->d_bsorted);
   if (h->d_bbins) cudaFree(h->d_bbins);
   if (h->d_serve) cudaFree(h->d_serve);
+  if (h->d_ftable) cudaFree(h->d_ftable);
   free_all(h->device_allocs);
+  if (h->host_arena) cudaFreeHost(h->host_arena);
   delete h;
   if (e != cudaSuccess) return galcapi::fail_cuda(e, "destroy sync");
   return GAL_OK;
@@ -284,6 +316,7 @@ extern "C" int gal_geometry(gal_allocator *h, gal_geometry_t *out) {
   out->total_slots = s.total_slots;
   out->num_classes = s.num_classes;
   for (uint32_t k = 0; k < s.num_classes; ++k) out->slot_count[k] = s.slot_count[k];
+  out->flags = s.flags;
   out->arena_base = (uint64_t)s.memory;
   return GAL_OK;
 }

@@ -34,6 +34,11 @@ struct gal_allocator {
   // scratch of the serving loop: slot and page tables
   void *d_serve;
   uint64_t d_serve_bytes;
+  // scratch of the host-buffer fused fill/drain: class trace and pointer table
+  uint64_t *d_ftable;
+  uint64_t d_ftable_bytes;
+  // GAL_FLAG_HOST_ARENA: the pinned host allocation behind hs.memory
+  char *host_arena;
 };
 
 struct gal_veb {

@@ -11,6 +11,7 @@ struct gal_device_alloc {
   __device__ __forceinline__ void free(void *p) { gal::free(&state, p); }
   __device__ __forceinline__ void *malloc_w(uint64_t n, uint32_t w) { return gal::malloc(&state, n, w); }
   __device__ __forceinline__ void free_w(void *p, uint32_t w) { gal::free(&state, p, w); }
+  __device__ __forceinline__ bool owns_allocation(const void *p) const { return gal::owns_allocation(&state, p); }
   // segments not in the segment tree (formatted for a tree or part of a
   // multi-segment allocation): a snapshot, read while others may change it
   __device__ inline uint64_t owned_segments() const {

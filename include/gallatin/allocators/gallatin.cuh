@@ -10,10 +10,17 @@
 // links against that library.
 //
 // Differences a user can see:
-//   * running_calloc is accepted and ignored: calloc through dynamic
-//     parallelism (reference gallatin.cuh:1306-1369) is not provided;
-//   * the arena is not zero-filled at creation (the reference memsets it,
-//     memory_table.cuh:518); like malloc, contents start undefined;
+//   * running_calloc zeroes on free inside the freeing warp (every lane that
+//     frees stores 16 B per step over each lane's allocation in turn) rather
+//     than in child grids launched through dynamic parallelism (reference
+//     gallatin.cuh:1306-1369); every tier is zeroed, slices included (the
+//     reference's block clear returns blocks without writing them,
+//     memory_table.cuh:101-136). A lone thread freeing a large allocation
+//     clears it alone: call free from the whole warp (other lanes may pass
+//     NULL) to share the work;
+//   * without running_calloc the arena is not zero-filled at creation (the
+//     reference memsets it, memory_table.cuh:518); like malloc, contents
+//     start undefined;
 //   * the geometry must satisfy biggest >= 32 * smallest.
 #ifndef GALLATIN_ALLOCATORS_GALLATIN_CUH
 #define GALLATIN_ALLOCATORS_GALLATIN_CUH
@@ -43,9 +50,20 @@ struct Gallatin {
 
   static __host__ my_type *generate_on_device(uint64_t max_bytes, uint64_t seed, bool print_info = true,
                                               bool running_calloc = false) {
-    (void)running_calloc;
+    return generate(max_bytes, seed, print_info, running_calloc ? GAL_FLAG_CALLOC : 0u);
+  }
+
+  // The same allocator over pinned host memory mapped into the GPU (the
+  // reference's generate_on_device_host, gallatin.cuh:423-526): the arena
+  // lives in host memory, the metadata in HBM.
+  static __host__ my_type *generate_on_device_host(uint64_t max_bytes, uint64_t seed, bool print_info = true,
+                                                   bool running_calloc = false) {
+    return generate(max_bytes, seed, print_info, GAL_FLAG_HOST_ARENA | (running_calloc ? GAL_FLAG_CALLOC : 0u));
+  }
+
+  static __host__ my_type *generate(uint64_t max_bytes, uint64_t seed, bool print_info, uint32_t flags) {
     gal_allocator *h = nullptr;
-    const int rc = gal_create(max_bytes, seed, bytes_per_segment, smallest, biggest, 0, &h);
+    const int rc = gal_create_ex(max_bytes, seed, bytes_per_segment, smallest, biggest, 0, flags, &h);
     if (rc != GAL_OK) {
       fprintf(stderr, "Gallatin: generate_on_device failed (%d): %s\n", rc, gal_last_error());
       return nullptr;
@@ -53,9 +71,9 @@ struct Gallatin {
     if (print_info) {
       gal_geometry_t g;
       gal_geometry(h, &g);
-      printf("Booted Gallatin with %u trees in range %llu-%llu and %f GB of memory %llu segments\n", g.num_trees,
+      printf("Booted Gallatin with %u trees in range %llu-%llu and %f GB of %s memory %llu segments\n", g.num_trees,
              (unsigned long long)smallest, (unsigned long long)biggest, 1.0 * max_bytes / 1024 / 1024 / 1024,
-             (unsigned long long)g.num_segments);
+             (flags & GAL_FLAG_HOST_ARENA) ? "pinned host" : "device", (unsigned long long)g.num_segments);
     }
     return reinterpret_cast<my_type *>(gal_device_state(h));
   }

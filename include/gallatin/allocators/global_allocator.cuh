@@ -1,9 +1,11 @@
 // Drop-in replacement for the reference's gallatin/allocators/global_allocator.cuh
-// (global_allocator.cuh:41-97): one default-typed allocator published through
-// a __device__ pointer, plus free functions. As in the reference, the
-// __device__ variable is defined in this header, so include it from one
-// translation unit (or compile with relocatable device code and include it
-// from exactly one).
+// (global_allocator.cuh:41-216): one default-typed allocator published through
+// a __device__ pointer, plus free functions; a second one over pinned host
+// memory (the _host functions); both together (_combined); and device-first
+// allocation that falls back to the host arena (_fused). As in the
+// reference, the __device__ variables are defined in this header, so include
+// it from one translation unit (or compile with relocatable device code and
+// include it from exactly one).
 #ifndef GALLATIN_ALLOCATORS_GLOBAL_ALLOCATOR_CUH
 #define GALLATIN_ALLOCATORS_GLOBAL_ALLOCATOR_CUH
 
@@ -15,6 +17,7 @@ namespace allocators {
 using global_allocator_type = gallatin::allocators::Gallatin<16ULL * 1024 * 1024, 16ULL, 4096ULL>;
 
 __device__ global_allocator_type *global_gallatin;
+__device__ global_allocator_type *global_host_gallatin;
 
 __host__ inline void init_global_allocator(uint64_t num_bytes, uint64_t seed, bool print_info = true,
                                            bool running_calloc = false) {
@@ -42,6 +45,78 @@ __host__ inline void print_global_stats() {
   cudaMemcpyFromSymbol(&local_copy, global_gallatin, sizeof(global_allocator_type *));
   cudaDeviceSynchronize();
   if (local_copy) local_copy->print_info();
+}
+
+// ---- the host-memory allocator (reference global_allocator.cuh:98-151) ----
+
+__host__ inline void init_global_allocator_host(uint64_t num_bytes, uint64_t seed, bool print_info = true,
+                                                bool running_calloc = false) {
+  global_allocator_type *local_copy =
+      global_allocator_type::generate_on_device_host(num_bytes, seed, print_info, running_calloc);
+  cudaMemcpyToSymbol(global_host_gallatin, &local_copy, sizeof(global_allocator_type *));
+  cudaDeviceSynchronize();
+}
+
+__host__ inline void free_global_allocator_host() {
+  global_allocator_type *local_copy = nullptr;
+  cudaMemcpyFromSymbol(&local_copy, global_host_gallatin, sizeof(global_allocator_type *));
+  cudaDeviceSynchronize();
+  if (local_copy) global_allocator_type::free_on_device(local_copy);
+  global_allocator_type *null_copy = nullptr;
+  cudaMemcpyToSymbol(global_host_gallatin, &null_copy, sizeof(global_allocator_type *));
+}
+
+__device__ inline void *global_malloc_host(uint64_t num_bytes) { return global_host_gallatin->malloc(num_bytes); }
+
+__device__ inline void global_free_host(void *ptr) { global_host_gallatin->free(ptr); }
+
+__host__ inline void print_global_stats_host() {
+  global_allocator_type *local_copy = nullptr;
+  cudaMemcpyFromSymbol(&local_copy, global_host_gallatin, sizeof(global_allocator_type *));
+  cudaDeviceSynchronize();
+  if (local_copy) local_copy->print_info();
+}
+
+// ---- both arenas (reference global_allocator.cuh:153-183) ----
+
+__host__ inline void init_global_allocator_combined(uint64_t num_bytes, uint64_t host_bytes, uint64_t seed,
+                                                    bool print_info = true, bool running_calloc = false) {
+  init_global_allocator(num_bytes, seed, print_info, running_calloc);
+  init_global_allocator_host(host_bytes, seed, print_info, running_calloc);
+}
+
+__host__ inline void free_global_allocator_combined() {
+  free_global_allocator();
+  free_global_allocator_host();
+}
+
+__device__ inline void *global_malloc_combined(uint64_t num_bytes, bool on_host = false) {
+  return on_host ? global_malloc_host(num_bytes) : global_malloc(num_bytes);
+}
+
+__device__ inline void global_free_combined(void *ptr, bool on_host = false) {
+  if (on_host) {
+    global_free_host(ptr);
+  } else {
+    global_free(ptr);
+  }
+}
+
+// ---- device first, host arena when the device arena is out of room
+//      (reference global_allocator.cuh:186-216); pointers stay where they
+//      were placed until freed ----
+
+__device__ inline void *global_malloc_fused(uint64_t num_bytes) {
+  void *alloc = global_malloc(num_bytes);
+  return alloc != nullptr ? alloc : global_malloc_host(num_bytes);
+}
+
+__device__ inline void global_free_fused(void *ptr) {
+  if (global_gallatin->owns_allocation(ptr)) {
+    global_free(ptr);
+  } else {
+    global_free_host(ptr);
+  }
 }
 
 }  // namespace allocators

@@ -46,8 +46,9 @@ typedef struct gal_geometry_t {
   uint32_t num_classes;               /* slot classes: num_trees - 1 single-slice
                                          trees, then one per run length 1, 2, 4 ...
                                          of the largest tree */
-  uint32_t pad_;
-  uint64_t arena_base; /* device address of the arena */
+  uint32_t flags;      /* GAL_FLAG_* the allocator was created with */
+  uint64_t arena_base; /* device address of the arena (with GAL_FLAG_HOST_ARENA
+                          also its host address: the mapping is the identity) */
 } gal_geometry_t;
 
 typedef struct gal_stats_t {
@@ -73,6 +74,21 @@ typedef struct gal_stats_t {
  * Replaces Gallatin<seg,min,max>::generate_on_device. */
 int gal_create(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size, uint64_t max_size,
                uint32_t min_slots, gal_allocator **out);
+
+/* gal_create with flags, a bit set of GAL_FLAG_HOST_ARENA and GAL_FLAG_CALLOC
+ * (state.h):
+ *   GAL_FLAG_HOST_ARENA  the arena is pinned, mapped host memory; the vEB
+ *                        trees, block words and bitmaps stay in HBM.
+ *                        Replaces Gallatin<...>::generate_on_device_host
+ *                        (reference gallatin.cuh:423-526, arena from
+ *                        memory_table.cuh:521-540).
+ *   GAL_FLAG_CALLOC      malloc returns zeroed bytes: the arena is zeroed
+ *                        here and every free zeroes what it returns before
+ *                        the bytes can be handed out again (reference
+ *                        running_calloc, gallatin.cuh:324-325,1306-1369).
+ * gal_create(...) is gal_create_ex(..., 0, out). */
+int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment_bytes, uint64_t min_size, uint64_t max_size,
+                  uint32_t min_slots, uint32_t flags, gal_allocator **out);
 
 /* Free everything, arena included (reference free_on_device, gallatin.cuh:643). */
 int gal_destroy(gal_allocator *h);
@@ -165,6 +181,38 @@ int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, ui
 int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
                                uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,
                                uint32_t block_dim, uint64_t *h_stats, void *stream);
+
+/* --- device-first allocation with a host-arena fallback ---
+ * The reference pairs a device allocator with one over pinned host memory
+ * and offers global_malloc_fused / global_free_fused: malloc from the device
+ * arena, and from the host arena when that returns NULL; free to whichever
+ * arena owns the pointer (global_allocator.cuh:128-216). This runs that
+ * pattern in the fill/drain shape of tests/src/global_exceed_test.cu:38-110.
+ * Fill (phase_mask bit 0): thread i mallocs 16 << class_i bytes (class_i =
+ * d_classes[i], or x mod 9 of xorshift64 seeded by splitmix64(seed + i) when
+ * d_classes is NULL), keeps the pointer in d_table[i] (n u64) and writes i
+ * to its first and ~i to its last u64. Drain (bit 1): thread i checks both
+ * words, frees d_table[i] and sets it to 0. host may be NULL (device arena
+ * only) and is normally a GAL_FLAG_HOST_ARENA allocator. stats: [0] NULLs,
+ * [1] verify failures, [4] allocations the host arena served. */
+int gal_run_fused(gal_allocator *dev, gal_allocator *host, uint64_t n, uint64_t seed, const uint8_t *d_classes,
+                  uint64_t *d_table, uint32_t phase_mask, unsigned long long *d_stats, void *stream);
+/* Both phases end to end from host memory: the class trace (n bytes) is
+ * copied in, the 8 stats words copied out, all on `stream`, then the stream
+ * is synchronised. The pointer table is scratch owned by `dev`. */
+int gal_run_fused_host(gal_allocator *dev, gal_allocator *host, uint64_t n, uint64_t seed, const uint8_t *h_classes,
+                       uint64_t *h_stats, void *stream);
+
+/* Zeroed-memory check for GAL_FLAG_CALLOC allocators (the property the
+ * reference's running_calloc mode is for, gallatin.cuh:1306-1369): each of
+ * n_threads threads, for `rounds` rounds, mallocs 16 << (x mod 12) bytes
+ * (single slices and multi-slice runs), checks that every byte reads zero,
+ * fills it with a non-zero pattern and frees it; warp 0 of every
+ * big_every-th CTA (256 threads) also takes one allocation of a size uniform
+ * in [big_lo, big_hi] per round through the same check (0 = none). stats:
+ * [0] NULLs, [1] allocations holding a non-zero byte. */
+int gal_run_zeroed(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed, uint32_t big_every,
+                   uint64_t big_lo, uint64_t big_hi, unsigned long long *d_stats, void *stream);
 
 /* --- batched request streams (no reference counterpart: the reference only
  *     serves per-thread calls from user kernels) ---

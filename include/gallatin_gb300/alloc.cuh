@@ -485,7 +485,8 @@ __device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint
 // still in flight holds a 0 that nobody can claim until it turns to 1; that
 // is what lets free_slice return bits and live count in either order.
 // The block holds no slice here, so any 0 bit is such a free: with none, the
-// block is pinned fresh and its first pass hands out slices by cursor alone.
+// block is pinned fresh and its first pass hands out slices by cursor (each
+// group still fetch-ands its bits: see malloc_slice).
 __device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t, uint32_t r) {
   const ulonglong2 *bits = reinterpret_cast<const ulonglong2 *>(st->block_bits + (b << 6));
   uint64_t all = ~0ull;
@@ -574,6 +575,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
     uint32_t take = 0;  // runs this attempt serves: the group, or what still fits
+    uint32_t lost = 0;  // fresh claim: group ranks whose run a bitmap claim took first
     bool nomem = false;
     bool busy = false;
     bool refill = false;
@@ -628,14 +630,32 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           cursor = meta_cursor(m);
           const uint32_t span = take * c;
           if ((m & GAL_META_FRESH_BIT) && cursor + span <= GAL_BLOCK_SLICES) {
-            // first pass of a fresh block: [cursor, cursor + span) is free
-            // and ours; clear those bits without waiting for the answer
+            // first pass of a fresh block: no other fresh claim gets
+            // [cursor, cursor + span), but a leader past the first pass
+            // claims from the bitmap and may reach these bits before this
+            // group clears them, so the bitmap decides: a run whose bits
+            // were already taken is lost to this group (what of it this
+            // fetch-and cleared goes back) and its lane tries again
             uint64_t *const fbits = st->block_bits + ((uint64_t)b << 6);
             for (uint32_t pos = cursor; pos < cursor + span;) {
               const uint32_t lo = pos & 63;
               const uint32_t n = 64 - lo < cursor + span - pos ? 64 - lo : cursor + span - pos;
-              ptx::red_and_relaxed(fbits + (pos >> 6), ~((n >= 64 ? ~0ull : ((1ull << n) - 1)) << lo));
+              const uint64_t mask = (n >= 64 ? ~0ull : ((1ull << n) - 1)) << lo;
+              const uint64_t old = ptx::atom_and_acquire(fbits + (pos >> 6), ~mask);
+              if ((old & mask) != mask) {
+                const uint64_t run = (c >= 64 ? ~0ull : ((1ull << c) - 1));
+                for (uint32_t q = pos; q < pos + n; q += c) {
+                  const uint64_t rm = run << (q & 63);
+                  if ((old & rm) == rm) continue;
+                  lost |= 1u << ((q - cursor) / c);
+                  if (old & rm) ptx::red_or_relaxed(fbits + (pos >> 6), old & rm);
+                }
+              }
               pos += n;
+            }
+            if (lost) {
+              release_live(st, b, (uint32_t)__popc(lost) * c);
+              count(st, GAL_CTR_CLAIM_SHORT);
             }
             cursor |= kFreshClaim;
           } else {
@@ -672,7 +692,8 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     if (b == GAL_EMPTY_BLOCK) continue;
     take = __shfl_sync(grp, take, leader);
     if (cursor & kFreshClaim) {  // the leader already holds these slices
-      if (g_rank < take) {
+      lost = __shfl_sync(grp, lost, leader);
+      if (g_rank < take && !((lost >> g_rank) & 1u)) {
         const uint64_t slice = (cursor & ~kFreshClaim) + g_rank * c;
         result = block_address(st, b, t) + (slice << (st->min_shift + (int)t));
         done = true;
@@ -826,6 +847,52 @@ __device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_
   veb::return_run(&st->segment_tree, seg, n);
 }
 
+// ---- zeroing for GAL_FLAG_CALLOC ------------------------------------------
+
+// Zero [p, p + bytes) for every lane of `active` with bytes != 0; the lanes
+// of `active` store 16 B each per step, one lane's range at a time, so a full
+// warp writes 512 contiguous bytes per step. bytes is a multiple of 16 and p
+// 16-byte aligned (every allocation is). Ends with the lanes' stores ordered
+// before anything each lane does next (__syncwarp orders memory among the
+// lanes it joins, so one lane's later release fence covers them all).
+__device__ inline void zero_ranges(uint32_t active, char *p, uint64_t bytes) {
+  const uint32_t lane = ptx::laneid();
+  const uint32_t rank = (uint32_t)__popc(active & ((1u << lane) - 1u));
+  const uint32_t group = (uint32_t)__popc(active);
+  uint32_t pending = __ballot_sync(active, bytes != 0);
+  while (pending) {
+    const int src = __ffs((int)pending) - 1;
+    pending &= pending - 1;
+    uint4 *q = (uint4 *)__shfl_sync(active, (unsigned long long)p, src);
+    const uint64_t n16 = __shfl_sync(active, (unsigned long long)bytes, src) >> 4;
+    for (uint64_t i = rank; i < n16; i += group) q[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncwarp(active);
+}
+
+// Bytes a live allocation at arena offset `off` spans, read from the
+// metadata that free uses (0 for a pointer free would reject): the slice run
+// of its block, a whole block-tier block, or its segments.
+__device__ inline uint64_t allocation_span(const gal_state_t *st, uint64_t off) {
+  if (off >= st->arena_bytes) return 0;
+  const uint64_t seg = off >> st->segment_shift;
+  const uint16_t id = st->chunk_ids[seg];
+  if (id < (uint16_t)st->num_trees) {
+    const uint32_t t = id;
+    const uint64_t b = (seg << block_index_shift(st)) + ((off & (st->segment_bytes - 1)) >> (st->block_shift_min + (int)t));
+    // state (WHOLE or not) and run length cannot change while the allocation
+    // is live; read past L1 all the same
+    const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
+    const int slice_shift = st->min_shift + (int)t;
+    if (meta_state(m) == GAL_STATE_WHOLE) return (uint64_t)GAL_BLOCK_SLICES << slice_shift;
+    const uint64_t c = (t == (uint32_t)st->num_trees - 1) ? (1ull << meta_run(m)) : 1ull;
+    return c << slice_shift;
+  }
+  if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees)
+    return ((uint64_t)id - (uint64_t)st->num_trees - 1) << st->segment_shift;
+  return 0;
+}
+
 // ---- public entry points -------------------------------------------------
 
 // `width` limits warp aggregation to tiles of 8, 16 or 32 lanes (the
@@ -839,6 +906,11 @@ __device__ __forceinline__ void *malloc(const gal_state_t *st, uint64_t size, ui
 }
 
 __device__ inline void free(const gal_state_t *st, void *ptr, uint32_t width = 32) {
+  // calloc mode: the freeing lanes zero their allocations together before
+  // any of them hands its bytes back (st->flags is the same for every lane)
+  if (st->flags & GAL_FLAG_CALLOC)
+    zero_ranges(__activemask(), (char *)ptr,
+                ptr == nullptr ? 0 : allocation_span(st, (uint64_t)((char *)ptr - st->memory)));
   if (ptr == nullptr) return;
   const uint64_t off = (uint64_t)((char *)ptr - st->memory);
   if (off >= st->arena_bytes) {

@@ -6,7 +6,9 @@
  * Everything here is plain C so that host code without nvcc can see it.
  *
  * HBM layout (all arrays are separate cudaMalloc allocations, 256-B aligned):
- *   memory          arena, num_segments * segment_bytes
+ *   memory          arena, num_segments * segment_bytes (with
+ *                   GAL_FLAG_HOST_ARENA: pinned, mapped host memory the GPU
+ *                   reaches over the C2C link; the metadata stays in HBM)
  *   chunk_ids       u16[num_segments]   0xFFFF = unformatted, t < num_trees =
  *                   formatted for slice tree t, num_trees+1+n = head of an
  *                   n-segment allocation (reference memory_table.cuh:823-851,
@@ -72,6 +74,12 @@
 /* a detached block is listed for early reuse once live <= this */
 #define GAL_ROOMY_MARK (GAL_BLOCK_SLICES / 2)
 
+/* gal_state_t.flags */
+#define GAL_FLAG_HOST_ARENA 1u /* arena in pinned host memory (reference host_only, memory_table.cuh:521-540) */
+#define GAL_FLAG_CALLOC 2u     /* arena zeroed at creation and every free zeroes its bytes before they
+                                  can be handed out again, so malloc returns zeroed memory (reference
+                                  running_calloc, gallatin.cuh:1306-1369) */
+
 /* slot word: low 32 bits block id (GAL_EMPTY_BLOCK when none), bit 32 set
  * while one leader is replacing the block. */
 #define GAL_SLOT_REPLACING (1ull << 32)
@@ -127,6 +135,7 @@ typedef struct gal_state_t {
   uint32_t num_classes;            /* slot classes, see above */
   uint32_t num_sms;
   uint32_t total_slots;
+  uint32_t flags;                  /* GAL_FLAG_* */
   uint32_t slot_count[GAL_MAX_TREES];
   uint32_t slot_offset[GAL_MAX_TREES];
   uint64_t seed;

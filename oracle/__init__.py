@@ -85,6 +85,12 @@ def load_replay():
         ]
         lib.cpu_replay_pairs.restype = c_double
         lib.cpu_replay_pairs.argtypes = [c_uint64, c_uint64, c_int, POINTER(c_uint64), POINTER(c_uint64)]
+        lib.cpu_replay_mixed_zeroed.restype = c_double
+        lib.cpu_replay_mixed_zeroed.argtypes = [c_uint64, c_uint64, c_uint64, c_uint32, c_uint64, c_void_p, c_int,
+                                                POINTER(c_uint64), POINTER(c_uint64)]
+        lib.cpu_replay_fill_drain.restype = c_double
+        lib.cpu_replay_fill_drain.argtypes = [c_uint64, c_void_p, c_void_p, c_int, POINTER(c_uint64),
+                                              POINTER(c_uint64)]
         lib.cpu_replay_batches.restype = c_double
         lib.cpu_replay_batches.argtypes = [c_void_p, c_void_p, c_uint32, c_void_p, c_int, POINTER(c_uint64)]
         lib.cpu_mixed_classes.restype = None
@@ -171,6 +177,27 @@ def cpu_replay_serving(trace: dict, admit_step: np.ndarray, *, page_bytes: int =
     return secs, checksum[:n], hist, nulls.value
 
 
+def cpu_replay_mixed_zeroed(n, tid_begin, tid_end, rounds, seed, *, workers=1, classes: np.ndarray | None = None):
+    """The mixed workload through glibc calloc, checking each allocation reads
+    zero; returns (seconds, misses, non-zero allocations)."""
+    misses, bad = c_uint64(0), c_uint64(0)
+    ptr = classes.ctypes.data if classes is not None else None
+    secs = load_replay().cpu_replay_mixed_zeroed(n, tid_begin, tid_end, rounds, seed, ptr, workers,
+                                                 ctypes.byref(misses), ctypes.byref(bad))
+    return secs, misses.value, bad.value
+
+
+def cpu_replay_fill_drain(classes: np.ndarray, workers: int = 1):
+    """glibc malloc for every class of the trace (fill), then verify and free
+    (drain); returns (seconds, misses, verify failures)."""
+    classes = np.ascontiguousarray(classes, dtype=np.uint8)
+    table = np.zeros(len(classes), dtype=np.uint64)
+    misses, bad = c_uint64(0), c_uint64(0)
+    secs = load_replay().cpu_replay_fill_drain(len(classes), classes.ctypes.data, table.ctypes.data, workers,
+                                               ctypes.byref(misses), ctypes.byref(bad))
+    return secs, misses.value, bad.value
+
+
 def cpu_replay_pairs(n, size, workers=1):
     misses, bad = c_uint64(0), c_uint64(0)
     secs = load_replay().cpu_replay_pairs(n, size, workers, ctypes.byref(misses), ctypes.byref(bad))
@@ -210,6 +237,8 @@ def _bind_ref(lib):
         "galref_veb_dump": (i32, [vp, i32, vp]),
         "galref_veb_run_ops": (i32, [vp, vp, u64, vp, vp]),
         "galref_create": (i32, [u64, u64, u64, u64, u64, POINTER(vp)]),
+        "galref_create_host": (i32, [u64, u64, u64, u64, u64, POINTER(vp)]),
+        "galref_run_fused": (i32, [vp, vp, u64, u64, vp, vp, u32, vp, vp]),
         "galref_destroy": (i32, [vp]),
         "galref_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
         "galref_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
@@ -260,15 +289,25 @@ class RefVeb:
 class RefGallatin:
     """The reference Gallatin<seg,min,max> on the GPU behind the shared workloads."""
 
-    def __init__(self, max_bytes: int, seed: int, segment_size=16 << 20, min_size=16, max_size=4096):
+    def __init__(self, max_bytes: int, seed: int, segment_size=16 << 20, min_size=16, max_size=4096, *,
+                 host_arena: bool = False):
+        """host_arena: the reference's generate_on_device_host (pinned host arena)."""
         lib = load_ref()
         if lib is None:
             raise RuntimeError("reference build unavailable")
         h = c_void_p()
-        rc = lib.galref_create(max_bytes, seed, segment_size, min_size, max_size, ctypes.byref(h))
+        create = lib.galref_create_host if host_arena else lib.galref_create
+        rc = create(max_bytes, seed, segment_size, min_size, max_size, ctypes.byref(h))
         if rc != 0:
-            raise RuntimeError(f"galref_create failed ({rc})")
+            raise RuntimeError(f"galref_create{'_host' if host_arena else ''} failed ({rc})")
         self._lib, self._h = lib, h.value
+
+    def run_fused(self, host, n, seed, d_table, d_stats, *, d_classes=0, phases=3, stream=0):
+        """Fill/drain through the reference's fused pattern (device first, then `host`)."""
+        rc = self._lib.galref_run_fused(self._h, host._h if host is not None else None, n, seed, d_classes, d_table,
+                                        phases, d_stats, stream)
+        if rc != 0:
+            raise RuntimeError(f"galref_run_fused failed ({rc})")
 
     def run_pairs(self, n, size, d_stats, block_dim=1024, stream=0):
         if self._lib.galref_run_pairs(self._h, n, size, block_dim, d_stats, stream) != 0:

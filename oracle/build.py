@@ -103,7 +103,7 @@ def build_reference(force: bool = False) -> bool:
     if not Path(nvcc).exists():
         return False
     src = ORACLE_DIR / "ref_harness.cu"
-    deps = [src, REPO_DIR / "gallatin_gb300" / "csrc" / "workloads.cuh"]
+    deps = [src, *(REPO_DIR / "gallatin_gb300" / "csrc").glob("*.cuh")]
     deps += list((REF_INCLUDE / "gallatin" / "allocators").glob("*.cuh"))
     if not force and not _stale(ref_lib(), deps):
         return True

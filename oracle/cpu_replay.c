@@ -38,6 +38,8 @@ typedef struct {
   uint32_t seg_every, block_dim;
   uint64_t seg_lo, seg_hi;
   uint64_t size; /* pairs workload when rounds == 0 */
+  int zeroed;    /* mixed: calloc, and check every byte reads zero first */
+  uint64_t *table; /* fill/drain: one pointer per thread id */
   uint64_t misses, bad;
 } job;
 
@@ -61,13 +63,18 @@ static void *run_mixed(void *arg) {
     for (uint32_t r = 0; r < j->rounds; ++r) {
       uint32_t cls = j->classes ? j->classes[(uint64_t)r * j->n + tid] : (uint32_t)(xorshift64(&s) % 9);
       uint64_t size = 16ull << cls;
-      uint64_t *p = (uint64_t *)malloc(size);
+      uint64_t *p = (uint64_t *)(j->zeroed ? calloc(1, size) : malloc(size));
       if (!p) {
         misses++;
         continue;
       }
       uint64_t v = tid ^ r;
       uint64_t words = size / 8;
+      if (j->zeroed) {
+        uint64_t seen = 0;
+        for (uint64_t i = 0; i < words; ++i) seen |= ((volatile uint64_t *)p)[i];
+        if (seen) bad++;
+      }
       for (uint64_t i = 0; i < words; ++i) p[i] = v;
       volatile uint64_t *vp = p;
       for (uint64_t i = 0; i < words; ++i) {
@@ -98,6 +105,42 @@ static void *run_pairs(void *arg) {
     free(p);
   }
   j->misses = misses;
+  j->bad = bad;
+  return NULL;
+}
+
+/* the fused fill/drain workload of gallatin_gb300/csrc/spill_workloads.cuh:
+ * thread i's size is 16 << classes[i]; fill writes i and ~i to the first and
+ * last u64, drain checks them and frees */
+static void *run_fill(void *arg) {
+  job *j = (job *)arg;
+  uint64_t misses = 0;
+  for (uint64_t i = j->begin; i < j->end; ++i) {
+    uint64_t size = 16ull << j->classes[i];
+    uint64_t *p = (uint64_t *)malloc(size);
+    j->table[i] = (uint64_t)p;
+    if (!p) {
+      misses++;
+      continue;
+    }
+    p[0] = i;
+    p[size / 8 - 1] = ~i;
+  }
+  j->misses = misses;
+  return NULL;
+}
+
+static void *run_drain(void *arg) {
+  job *j = (job *)arg;
+  uint64_t bad = 0;
+  for (uint64_t i = j->begin; i < j->end; ++i) {
+    uint64_t *p = (uint64_t *)j->table[i];
+    if (!p) continue;
+    uint64_t size = 16ull << j->classes[i];
+    if (((volatile uint64_t *)p)[0] != i || ((volatile uint64_t *)p)[size / 8 - 1] != ~i) bad++;
+    free(p);
+    j->table[i] = 0;
+  }
   j->bad = bad;
   return NULL;
 }
@@ -162,6 +205,42 @@ double cpu_replay_pairs(uint64_t n, uint64_t size, int workers, uint64_t *misses
   proto.n = n;
   proto.size = size;
   return run_jobs(run_pairs, &proto, workers, misses, bad);
+}
+
+/* The mixed workload through calloc: every allocation is checked to read
+ * zero before the fill (bad counts those that did not). */
+double cpu_replay_mixed_zeroed(uint64_t n, uint64_t tid_begin, uint64_t tid_end, uint32_t rounds, uint64_t seed,
+                               const uint8_t *classes, int workers, uint64_t *misses, uint64_t *bad) {
+  job proto;
+  memset(&proto, 0, sizeof(proto));
+  proto.begin = tid_begin;
+  proto.end = tid_end;
+  proto.n = n;
+  proto.rounds = rounds;
+  proto.seed = seed;
+  proto.classes = classes;
+  proto.block_dim = 256;
+  proto.zeroed = 1;
+  return run_jobs(run_mixed, &proto, workers, misses, bad);
+}
+
+/* Fill then drain n allocations (table: n u64 the caller provides); returns
+ * the wall seconds of both phases. */
+double cpu_replay_fill_drain(uint64_t n, const uint8_t *classes, uint64_t *table, int workers, uint64_t *misses,
+                             uint64_t *bad) {
+  job proto;
+  memset(&proto, 0, sizeof(proto));
+  proto.begin = 0;
+  proto.end = n;
+  proto.n = n;
+  proto.classes = classes;
+  proto.table = table;
+  uint64_t m = 0, b = 0, m2 = 0, b2 = 0;
+  double secs = run_jobs(run_fill, &proto, workers, &m, &b);
+  secs += run_jobs(run_drain, &proto, workers, &m2, &b2);
+  *misses = m;
+  *bad = b2;
+  return secs;
 }
 
 /* The class trace the mixed workload draws: classes[r * n + tid]. */

@@ -8,7 +8,10 @@
 //     runner the GB300 library has, to produce golden vectors;
 //   * the reference Gallatin<seg,min,max> (gallatin.cuh:292) behind the same
 //     workload kernels (gallatin_gb300/csrc/workloads.cuh) the GB300 library
-//     runs, for the reference arm of bench.py.
+//     runs, for the reference arm of bench.py;
+//   * its host-memory form (generate_on_device_host, gallatin.cuh:423-526)
+//     paired with a device one behind the fused fill/drain kernels
+//     (gallatin_gb300/csrc/spill_workloads.cuh).
 #include <gallatin/allocators/gallatin.cuh>
 
 #include <cuda_runtime.h>
@@ -18,6 +21,7 @@
 #include "gallatin_gb300.h"  // gal_veb_op layout, op codes and serving structs only
 #include "ds_workloads.cuh"
 #include "serving.cuh"
+#include "spill_workloads.cuh"
 #include "workloads.cuh"
 
 using namespace gallatin::allocators;
@@ -145,6 +149,16 @@ int launch_serving(void *dev, const galserve::server_t &sv, const galserve::trac
   cudaGetDeviceProperties(&prop, dev_id);
   // the plain path (mode 0): one launch per phase per step
   return galserve::run((G *)dev, sv, t, p, o, 0, 4u * prop.multiProcessorCount, s) == cudaSuccess ? 0 : 2;
+}
+
+template <class G>
+int launch_fused(void *dev, void *host, uint64_t n, uint64_t seed, const uint8_t *classes, uint64_t *table,
+                 uint32_t phases, unsigned long long *stats, cudaStream_t s) {
+  galwork::fused_alloc<G> f{(G *)dev, (G *)host};
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (phases & 1u) galwork::fill_kernel<G><<<grid, 256, 0, s>>>(f, n, seed, classes, table, stats);
+  if (phases & 2u) galwork::drain_kernel<G><<<grid, 256, 0, s>>>(f, n, seed, classes, table, stats);
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 template <class G>
@@ -299,6 +313,54 @@ int galref_create(uint64_t max_bytes, uint64_t seed, uint64_t seg, uint64_t mn, 
   cudaMemset(a->d_stats, 0, 64);
   *out = a;
   return cudaDeviceSynchronize() == cudaSuccess ? 0 : 2;
+}
+
+// The reference allocator over pinned host memory. Its generate_on_device_host
+// sets cudaDeviceMapHost and exits the process if that fails
+// (gallatin.cuh:437), so the flag is tried here first and a failure is
+// returned instead.
+int galref_create_host(uint64_t max_bytes, uint64_t seed, uint64_t seg, uint64_t mn, uint64_t mx, void **out) {
+  const int config = config_of(seg, mn, mx);
+  if (config < 0) return 1;
+  if (cudaSetDeviceFlags(cudaDeviceMapHost) != cudaSuccess) {
+    cudaGetLastError();
+    return 4;
+  }
+  RefAlloc *a = new RefAlloc();
+  a->config = config;
+  a->d_classes = nullptr;
+  a->d_classes_bytes = 0;
+  a->d_serve = nullptr;
+  a->d_serve_bytes = 0;
+  switch (config) {
+    case 0: a->dev = ref_16m_16_4096::generate_on_device_host(max_bytes, seed, false); break;
+    case 1: a->dev = ref_16m_128_4096::generate_on_device_host(max_bytes, seed, false); break;
+    case 2: a->dev = ref_64m_16_4096::generate_on_device_host(max_bytes, seed, false); break;
+    default: a->dev = ref_4m_16_1024::generate_on_device_host(max_bytes, seed, false); break;
+  }
+  if (cudaMalloc(&a->d_stats, 64) != cudaSuccess) return 3;
+  cudaMemset(a->d_stats, 0, 64);
+  *out = a;
+  return cudaDeviceSynchronize() == cudaSuccess ? 0 : 2;
+}
+
+// Device first, host arena when the device returns NULL (the reference's
+// global_malloc_fused / global_free_fused, global_allocator.cuh:186-216), in
+// the fill/drain shape; dev and host must share a configuration.
+int galref_run_fused(void *dev_h, void *host_h, uint64_t n, uint64_t seed, const uint8_t *d_classes,
+                     uint64_t *d_table, uint32_t phases, unsigned long long *d_stats, void *stream) {
+  RefAlloc *a = (RefAlloc *)dev_h;
+  RefAlloc *b = (RefAlloc *)host_h;
+  if (b != nullptr && b->config != a->config) return 1;
+  void *host = b ? b->dev : nullptr;
+  if (n == 0) return 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a->config) {
+    case 0: return launch_fused<ref_16m_16_4096>(a->dev, host, n, seed, d_classes, d_table, phases, d_stats, s);
+    case 1: return launch_fused<ref_16m_128_4096>(a->dev, host, n, seed, d_classes, d_table, phases, d_stats, s);
+    case 2: return launch_fused<ref_64m_16_4096>(a->dev, host, n, seed, d_classes, d_table, phases, d_stats, s);
+    default: return launch_fused<ref_4m_16_1024>(a->dev, host, n, seed, d_classes, d_table, phases, d_stats, s);
+  }
 }
 
 int galref_destroy(void *h) {

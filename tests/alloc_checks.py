@@ -44,6 +44,17 @@ def check_alignment_and_bounds(alloc: gal.Gallatin, spans) -> None:
         assert (s - base) % align == 0, f"size {size} at offset {s - base:#x} not aligned to {align}"
 
 
+def _block_state(alloc: gal.Gallatin, off: int, tree: int) -> str:
+    """The meta word fields of the block holding arena offset `off` (for failure messages)."""
+    seg_shift = alloc.segment_size.bit_length() - 1
+    block_shift = alloc.min_size.bit_length() - 1 + 12
+    b = ((off >> seg_shift) << (seg_shift - block_shift)) + ((off & (alloc.segment_size - 1)) >> (block_shift + tree))
+    m = int(alloc.dump("block_meta")[b])
+    counters = {k: v for k, v in alloc.stats()["counters"].items() if v}
+    return (f"block {b}: live {m & 0xFFFFFFFF} tree {(m >> 32) & 0xFF} state {(m >> 40) & 3} run {(m >> 42) & 15} "
+            f"flags {(m >> 46) & 3} cursor {m >> 48}; counters {counters}")
+
+
 def check_size_classes(alloc: gal.Gallatin, spans) -> None:
     ids = alloc.dump("chunk_ids")
     seg_shift = alloc.segment_size.bit_length() - 1
@@ -51,7 +62,12 @@ def check_size_classes(alloc: gal.Gallatin, spans) -> None:
         seg = (s - alloc.arena_base) >> seg_shift
         tier, tree, cnt = gal.classify(size, alloc.min_size, alloc.max_size, alloc.segment_size)
         want = alloc.num_trees + 1 + cnt if tier == "segment" else tree
-        assert int(ids[seg]) == want, f"size {size}: segment {seg} tagged {int(ids[seg])}, want {want}"
+        if int(ids[seg]) != want:
+            bad = sum(1 for s2, _, z2 in spans if int(ids[(s2 - alloc.arena_base) >> seg_shift]) == gal.GAL_FREE_SEGMENT)
+            detail = _block_state(alloc, s - alloc.arena_base, tree) if tier == "slice" else ""
+            raise AssertionError(f"size {size} at offset {s - alloc.arena_base:#x}: segment {seg} tagged "
+                                 f"{int(ids[seg])}, want {want} ({bad} allocations in untagged segments; "
+                                 f"tags {ids.tolist()[:48]}); {detail}")
 
 
 def check_live(alloc, ptrs, sizes) -> list:

@@ -49,3 +49,24 @@ def test_invalid_geometry_is_rejected_without_touching_the_gpu():
         gal.Gallatin.generate_on_device(1 << 30, 1, print_info=False, min_size=64, max_size=1024)
     with pytest.raises(gal.GalError, match="segment"):
         gal.Gallatin.generate_on_device(1 << 30, 1, print_info=False, segment_size=1 << 20, max_size=4096)
+
+
+def test_create_ex_rejects_unknown_flags_without_touching_the_gpu():
+    import ctypes
+
+    import gallatin_gb300 as gal
+
+    lib = gal.load()
+    h = ctypes.c_void_p()
+    rc = lib.gal_create_ex(1 << 30, 1, 16 << 20, 16, 4096, 0, 0x80, ctypes.byref(h))
+    assert rc == 1 and not h.value
+    assert b"flags" in lib.gal_last_error()
+
+
+def test_owns_allocation_is_the_arena_range():
+    import gallatin_gb300 as gal
+
+    a = object.__new__(gal.Gallatin)  # the range test needs no device state
+    a.arena_base, a.arena_bytes = 1 << 40, 64 << 20
+    assert a.owns_allocation(1 << 40) and a.owns_allocation((1 << 40) + (64 << 20) - 16)
+    assert not a.owns_allocation((1 << 40) + (64 << 20)) and not a.owns_allocation((1 << 40) - 16)
