@@ -220,6 +220,7 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
   if ((rc = device_alloc(h, &s.block_bits, nblocks * 64, "cudaMalloc block_bits")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.slots, total, "cudaMalloc slots")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.locks, 1, "cudaMalloc locks")) != GAL_OK) return cleanup(rc);
+  if ((rc = device_alloc(h, &s.nomem, 1, "cudaMalloc nomem")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &s.counters, GAL_NUM_COUNTERS, "cudaMalloc counters")) != GAL_OK) return cleanup(rc);
   if ((rc = device_alloc(h, &h->d_stats, 8, "cudaMalloc stats")) != GAL_OK) return cleanup(rc);
 
@@ -233,6 +234,7 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
       // every slice starts free; the bitmap is never rewritten afterwards
       (rc = try_cuda(cudaMemset(s.block_bits, 0xFF, nblocks * 64 * 8), "memset block_bits")) ||
       (rc = try_cuda(cudaMemset(s.locks, 0, sizeof(uint32_t)), "memset locks")) ||
+      (rc = try_cuda(cudaMemset(s.nomem, 0, sizeof(uint32_t)), "memset nomem")) ||
       (rc = try_cuda(cudaMemset(s.counters, 0, GAL_NUM_COUNTERS * 8), "memset counters")) ||
       (rc = try_cuda(cudaMemset(h->d_stats, 0, 64), "memset stats")))
     return cleanup(rc);

@@ -55,6 +55,7 @@ extern "C" int gal_flush_pinned(gal_allocator *h, void *stream) {
   const uint32_t total = h->hs.total_slots;
   flush_kernel<<<grid_for(total, 128), 128, 0, as_stream(stream)>>>(h->d_state, total);
   GAL_CUDA_TRY(cudaGetLastError(), "flush launch");
+  GAL_CUDA_TRY(cudaMemsetAsync(h->hs.nomem, 0, sizeof(uint32_t), as_stream(stream)), "nomem reset");
   return GAL_OK;
 }
 

@@ -515,15 +515,21 @@ __device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) 
 // another pinned one. Only the thread whose CAS sets REPLACING does the work;
 // REPLACE_NOMEM when request_block found nothing (the slot is left as seen).
 __device__ inline int replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t, uint32_t r,
-                                   uint64_t tid, int adopt_mode, uint32_t *out) {
+                                   int adopt_mode, uint32_t *out) {
+  // the hashed search starts come from the thread id, read here rather than
+  // carried through the claim loop
+  const uint64_t tid = veb::thread_tid();
   *out = GAL_EMPTY_BLOCK;
   if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return REPLACE_BUSY;
   bool adopted = false;
   const uint32_t nb = request_block(st, t, t + r, 1u << r, tid, adopt_mode, &adopted);
+  const uint32_t kbit = 1u << (t + r);
   if (nb == GAL_EMPTY_BLOCK) {
     ptx::st_release(slot, seen);
+    if (adopt_mode == ADOPT_ANY && !(ptx::ld_relaxed(st->nomem) & kbit)) atomicOr(st->nomem, kbit);
     return REPLACE_NOMEM;
   }
+  if (ptx::ld_relaxed(st->nomem) & kbit) atomicAnd(st->nomem, ~kbit);
   if (!adopted) pin_block(st, nb, t, r);
   ptx::st_release(slot, (uint64_t)nb);
   if ((uint32_t)seen != GAL_EMPTY_BLOCK) detach_block(st, (uint32_t)seen);
@@ -543,10 +549,12 @@ __device__ __forceinline__ uint32_t tile_mask(uint32_t width) {
 // Warp-aggregated slice allocation of one run of 2^r slices of tree t. Lanes
 // asking for the same class form one group; its leader reserves the group's
 // total with one atomic on the pinned block's meta word and claims bits with
-// fetch-and. A group that finds every slot of its class full while the arena
-// has no block to replace them gives up (nullptr) instead of retrying.
-__device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t r, uint64_t tid,
-                                     uint32_t width = 32) {
+// fetch-and. Once a replacement finds no block in the arena for the class
+// (or the group meets a slot being replaced while the last replacement for
+// the class found none), the group asks for no more blocks: each further slot
+// it finds full or empty is a strike, and after a strike on every slot the
+// arena cannot serve the class now (nullptr).
+__device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t, uint32_t r, uint32_t width = 32) {
   const uint32_t c = 1u << r;
   const uint32_t k = t + r;
   const uint32_t active = __activemask();
@@ -560,8 +568,8 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   const uint32_t tag = t | (GAL_STATE_PINNED << (GAL_META_STATE_SHIFT - 32)) | (r << (GAL_META_RUN_SHIFT - 32));
   void *result = nullptr;
   bool done = false;
-  uint32_t strikes = 0;  // slots found full with no block to replace them
   uint32_t hops = 0;     // slots passed over while another leader replaced their block
+  uint32_t strikes = 0;  // slots found full or empty once the arena had no block for the class
   for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
     const uint32_t grp = __ballot_sync(peers, !done);
     if (grp == 0) break;
@@ -584,12 +592,15 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
       const bool replacing = (sv & GAL_SLOT_REPLACING) != 0;
       b = (uint32_t)sv;
       if (b == GAL_EMPTY_BLOCK) {
-        if (!replacing) {
+        if (strikes) {
+          nomem = true;  // the arena had no block for the class: do not ask again
+        } else if (!replacing) {
           count(st, GAL_CTR_REPLACE_EMPTY);
-          nomem = replace_slot(st, slot, sv, t, r, tid, ADOPT_ANY, &b) == REPLACE_NOMEM;
+          nomem = replace_slot(st, slot, sv, t, r, ADOPT_ANY, &b) == REPLACE_NOMEM;
         } else {
           count(st, GAL_CTR_SLOT_BUSY);
-          busy = true;
+          nomem = (ptx::ld_relaxed(st->nomem) >> k) & 1u;
+          busy = !nomem;
         }
       }
       if (b != GAL_EMPTY_BLOCK) {
@@ -614,16 +625,19 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
             }
           }
           if (take == 0) {
-            if (!replacing) {
+            if (strikes) {
+              nomem = true;  // the arena had no block for the class: do not ask again
+            } else if (!replacing) {
               count(st, GAL_CTR_REPLACE_FULL);
               uint32_t nb;
-              nomem = replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ANY, &nb) == REPLACE_NOMEM;
+              nomem = replace_slot(st, slot, (uint64_t)b, t, r, ADOPT_ANY, &nb) == REPLACE_NOMEM;
             } else {
               count(st, GAL_CTR_SLOT_BUSY);
-              busy = true;
+              nomem = (ptx::ld_relaxed(st->nomem) >> k) & 1u;
+              busy = !nomem;
             }
           }
-        } else if (!replacing && meta_live(m) + need > kRefillMark) {
+        } else if (!replacing && !strikes && meta_live(m) + need > kRefillMark) {
           refill = true;  // swap in another block once this group is served
         }
         if (take > 0) {
@@ -682,7 +696,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     b = __shfl_sync(grp, b, leader);
     cursor = __shfl_sync(grp, cursor, leader);
     if (b == kNoMemBlock) {
-      if (++strikes >= nslots) done = true;  // every slot tried: the arena cannot serve this class now
+      if (++strikes >= nslots) done = true;
       continue;
     }
     if (b == kBusyBlock) {
@@ -701,7 +715,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
       if (refill && lane == (uint32_t)leader) {
         count(st, GAL_CTR_REPLACE_REFILL);
         uint32_t nb;
-        replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ROOMY, &nb);  // no nearly-full blocks
+        replace_slot(st, slot, (uint64_t)b, t, r, ADOPT_ROOMY, &nb);  // no nearly-full blocks
       }
       continue;
     }
@@ -754,7 +768,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     if (refill && lane == (uint32_t)leader) {
       count(st, GAL_CTR_REPLACE_REFILL);
       uint32_t nb;
-      replace_slot(st, slot, (uint64_t)b, t, r, tid, ADOPT_ROOMY, &nb);  // no nearly-full blocks
+      replace_slot(st, slot, (uint64_t)b, t, r, ADOPT_ROOMY, &nb);  // no nearly-full blocks
     }
   }
   if (result == nullptr) count(st, GAL_CTR_OOM_SLICE);
@@ -899,9 +913,8 @@ __device__ inline uint64_t allocation_span(const gal_state_t *st, uint64_t off) 
 // reference groups the whole coalesced warp, gallatin.cuh:883-885).
 __device__ __forceinline__ void *malloc(const gal_state_t *st, uint64_t size, uint32_t width = 32) {
   const size_class sc = classify(st, size);
-  const uint64_t tid = veb::thread_tid();
-  if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, (uint32_t)(__ffs((int)sc.count) - 1), tid, width);
-  if (sc.tier == TIER_BLOCK) return malloc_block(st, sc.tree, tid);
+  if (sc.tier == TIER_SLICE) return malloc_slice(st, sc.tree, (uint32_t)(__ffs((int)sc.count) - 1), width);
+  if (sc.tier == TIER_BLOCK) return malloc_block(st, sc.tree, veb::thread_tid());
   return malloc_segment(st, sc.nseg);
 }
 

@@ -148,6 +148,8 @@ typedef struct gal_state_t {
   uint64_t *block_bits;
   uint64_t *slots;
   uint32_t *locks;                 /* bit t: tree t attach lock; bit 31: segment tier */
+  uint32_t *nomem;                 /* bit k: the last replacement for slot class k found no
+                                      block (a hint; cleared by the next one that does) */
   unsigned long long *counters;    /* GAL_NUM_COUNTERS */
 
   gal_veb_t segment_tree;
