@@ -154,3 +154,39 @@ def test_binned_path_serves_each_request_like_the_plain_path(cuda):
             check_live(a, table[live], sizes[live])
             tables.append(live)
     assert np.array_equal(tables[0], tables[1])
+
+
+@pytest.mark.parametrize("arena_mib,calloc,binned", [(64, False, False), (128, False, True), (64, True, True)],
+                         ids=["64MiB-plain", "128MiB-binned", "64MiB-calloc-binned"])
+def test_batches_in_an_arena_too_small_for_the_stream(cuda, arena_mib, calloc, binned):
+    # the stream's live set peaks near 90 MB in class bytes, over nine slice
+    # trees and the block tier: a 4- or 8-segment arena runs out. Mallocs
+    # return NULL (the strike path), what was served must still be a valid
+    # live set, frees of NULL slots are no-ops, and the drain restores the state
+    reqs, offsets, slots, info = small_trace(11)
+    with gal.Gallatin.generate_on_device(arena_mib << 20, 6, print_info=False, running_calloc=calloc) as a:
+        d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
+        d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
+        d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        a.run_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets[:-1], d_table.data_ptr(), stats.data_ptr(),
+                      persistent=binned, binned=binned)
+        cuda.cuda.synchronize()
+        assert int(stats[0]) > 0, "the arena should have run out"
+        table = d_table.cpu().numpy().view(np.uint64)
+        sizes = np.zeros(slots + 1, dtype=np.uint64)
+        for r in reqs[: int(offsets[-2])]:
+            slot, size = int(r >> np.uint64(32)), int(r & np.uint64(0xFFFFFFFF))
+            sizes[slot] = size
+        live = table != 0
+        assert live.any()
+        check_live(a, table[live], sizes[live])
+        drain = offsets[-2:]
+        d_drain = cuda.from_numpy((drain - drain[0]).view(np.int64)).cuda()
+        d_reqs_drain = cuda.from_numpy(reqs[int(drain[0]):].view(np.int64).copy()).cuda()
+        a.run_batches(d_reqs_drain.data_ptr(), d_drain.data_ptr(), drain - drain[0], d_table.data_ptr(),
+                      stats.data_ptr(), persistent=binned, binned=binned)
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        assert not d_table.any()
+        check_restored(a)

@@ -214,3 +214,23 @@ def test_calloc_batches_stream(cuda):
         check_restored(a)
     finally:
         a.free_on_device()
+
+
+@pytest.mark.parametrize("calloc", [False, True], ids=["plain", "calloc"])
+def test_mixed_rounds_in_a_full_arena_never_share_a_slice(cuda, calloc):
+    # 262,144 threads x 4 rounds of malloc / fill / verify / free against 4
+    # segments: most rounds find the arena full. Any slice handed to two
+    # owners at once shows up as a verify failure (each fills it with its own
+    # value and reads it back)
+    a = gal.Gallatin.generate_on_device(64 << 20, 31, print_info=False, running_calloc=calloc)
+    try:
+        d_stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        a.run_mixed(1 << 18, 4, 9, d_stats.data_ptr())
+        cuda.cuda.synchronize()
+        st = d_stats.cpu().numpy()
+        assert st[STAT_MISS] > 0 and st[STAT_BAD] == 0, st
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        check_restored(a)
+    finally:
+        a.free_on_device()
