@@ -103,7 +103,13 @@ def measured_peaks() -> dict:
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    """nvidia-smi clock / throttle-reason samples during the timed region.
+
+    Sampling starts before the region and the sampler waits for its first
+    sample, and it keeps sampling for a short while after the region, so a
+    region shorter than the 50 ms sampling period (the 16 B pairs workload
+    times well under a millisecond) is still bracketed by samples taken
+    next to it."""
 
     QUERY = (
         "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -114,8 +120,17 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.lines: list[str] = []
+        self._reader = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            if ln.strip():
+                self.lines.append(ln.strip())
 
     def __enter__(self):
+        import threading
+
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
@@ -124,19 +139,29 @@ class ClockSampler:
             )
         except OSError:
             self.proc = None
+            return self
+        self._reader = threading.Thread(target=self._read, daemon=True)
+        self._reader.start()
+        t0 = time.perf_counter()
+        while not self.lines and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):
-        if self.proc is not None:
-            self.proc.terminate()
-            try:
-                out, _ = self.proc.communicate(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [ln for ln in out.splitlines() if ln.strip()]
-        else:
-            self.lines = []
+        if self.proc is None:
+            return
+        n = len(self.lines)
+        t0 = time.perf_counter()
+        while len(self.lines) < n + 2 and time.perf_counter() - t0 < 1.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            self.proc.wait()
+        if self._reader is not None:
+            self._reader.join(timeout=5)
 
     def summary(self) -> dict:
         sms, maxes, reasons = [], [], set()

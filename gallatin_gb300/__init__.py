@@ -208,6 +208,7 @@ def load(path: str | Path | None = None):
         "gal_graph_destroy": (i32, [vp]),
         "gal_run_batches_host": (i32, [vp, vp, vp, u32, u64, u32, u32, u32, vp, vp]),
         "gal_run_serving": (i32, [vp, vp, vp, vp, vp]),
+        "gal_run_serving_fused": (i32, [vp, vp, vp, vp, vp, vp]),
         "gal_table_create": (i32, [vp, u64, u64, POINTER(vp)]),
         "gal_table_op": (i32, [vp, u32, vp, u64, u64, vp, vp]),
         "gal_table_chain_stats": (i32, [vp, POINTER(u64), POINTER(u64)]),
@@ -523,6 +524,12 @@ class Gallatin:
         """gal_run_serving on this allocator (pointers to the structs of
         gallatin_gb300.serving); returns 0 or raises GalError."""
         _check(load().gal_run_serving(self.handle, trace_ptr, params_ptr, out_ptr, stream))
+        return 0
+
+    def run_serving_fused(self, host: "Gallatin", trace_ptr, params_ptr, out_ptr, stream: int = 0) -> int:
+        """gal_run_serving_fused: pages from this allocator first, from `host`
+        (a host-arena allocator) when it has none."""
+        _check(load().gal_run_serving_fused(self.handle, host.handle, trace_ptr, params_ptr, out_ptr, stream))
         return 0
 
     # -- data structures ------------------------------------------------------

@@ -141,6 +141,7 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
   h->d_ftable = nullptr;
   h->d_ftable_bytes = 0;
   h->host_arena = nullptr;
+  h->d_fused = nullptr;
   h->min_size = min_size;
   h->max_size = max_size;
   gal_state_t &s = h->hs;
@@ -288,6 +289,7 @@ extern "C" int gal_destroy(gal_allocator *h) {
   if (h->d_bbins) cudaFree(h->d_bbins);
   if (h->d_serve) cudaFree(h->d_serve);
   if (h->d_ftable) cudaFree(h->d_ftable);
+  if (h->d_fused) cudaFree(h->d_fused);
   free_all(h->device_allocs);
   if (h->host_arena) cudaFreeHost(h->host_arena);
   delete h;

@@ -39,6 +39,9 @@ struct gal_allocator {
   uint64_t d_ftable_bytes;
   // GAL_FLAG_HOST_ARENA: the pinned host allocation behind hs.memory
   char *host_arena;
+  // the device-side pair (this allocator, a host-arena one) of the fused
+  // serving loop, written before each such run
+  void *d_fused;
 };
 
 struct gal_veb {

@@ -25,11 +25,11 @@ int check_params(const gal_serve_trace_t *tr, const gal_serve_params_t *pr, cons
 
 }  // namespace
 
-extern "C" int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *tr, const gal_serve_params_t *pr,
-                               const gal_serve_out_t *out, void *stream) {
-  if (h == nullptr) return galcapi::fail_invalid("handle is NULL");
-  int rc = check_params(tr, pr, out);
-  if (rc != GAL_OK) return rc;
+// Scratch, struct conversion and launch shared by both entry points; `a` is
+// the device-side allocator object the kernels receive.
+template <class A>
+int run_serving_on(gal_allocator *h, A *a, const gal_serve_trace_t *tr, const gal_serve_params_t *pr,
+                   const gal_serve_out_t *out, void *stream) {
   const galserve::layout_t l = galserve::layout(pr->max_slots, pr->max_pages);
   if (l.total > h->d_serve_bytes) {
     if (h->d_serve) cudaFree(h->d_serve);
@@ -44,14 +44,35 @@ extern "C" int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *tr, co
   galserve::out_t o{out->checksum, out->admit_step, out->finish_step, out->step_stats,
                     (unsigned long long *)out->latency_hist};
   int per_sm = 0;
-  GAL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, galserve::serve_persistent_kernel<gal_device_alloc>, 256, 0),
+  GAL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, galserve::serve_persistent_kernel<A>, 256, 0),
                "occupancy query");
   if (per_sm < 1) return galcapi::fail_invalid("serving kernel does not fit on an SM");
   if (pr->ctas_per_sm > (uint32_t)per_sm) return galcapi::fail_invalid("more CTAs per SM than fit");
   if (pr->ctas_per_sm) per_sm = (int)pr->ctas_per_sm;
-  GAL_CUDA_TRY(galserve::run(reinterpret_cast<gal_device_alloc *>(h->d_state), sv, t, p, o, pr->mode,
-                             (uint32_t)per_sm * h->hs.num_sms, (cudaStream_t)stream),
+  GAL_CUDA_TRY(galserve::run(a, sv, t, p, o, pr->mode, (uint32_t)per_sm * h->hs.num_sms, (cudaStream_t)stream),
                "serving launch");
   return GAL_OK;
+}
+
+extern "C" int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *tr, const gal_serve_params_t *pr,
+                               const gal_serve_out_t *out, void *stream) {
+  if (h == nullptr) return galcapi::fail_invalid("handle is NULL");
+  const int rc = check_params(tr, pr, out);
+  if (rc != GAL_OK) return rc;
+  return run_serving_on(h, reinterpret_cast<gal_device_alloc *>(h->d_state), tr, pr, out, stream);
+}
+
+extern "C" int gal_run_serving_fused(gal_allocator *dev, gal_allocator *host, const gal_serve_trace_t *tr,
+                                     const gal_serve_params_t *pr, const gal_serve_out_t *out, void *stream) {
+  if (dev == nullptr || host == nullptr) return galcapi::fail_invalid("handle is NULL");
+  if (dev == host) return galcapi::fail_invalid("the host allocator must be a second allocator");
+  if (dev->hs.segment_bytes != host->hs.segment_bytes)
+    return galcapi::fail_invalid("both allocators must use the same segment size");
+  const int rc = check_params(tr, pr, out);
+  if (rc != GAL_OK) return rc;
+  if (dev->d_fused == nullptr) GAL_CUDA_TRY(cudaMalloc(&dev->d_fused, sizeof(gal_fused_device_alloc)), "cudaMalloc fused");
+  const gal_fused_device_alloc f{reinterpret_cast<gal_device_alloc *>(dev->d_state),
+                                 reinterpret_cast<gal_device_alloc *>(host->d_state)};
+  GAL_CUDA_TRY(cudaMemcpy(dev->d_fused, &f, sizeof(f), cudaMemcpyHostToDevice), "fused pair H2D");
+  return run_serving_on(dev, reinterpret_cast<gal_fused_device_alloc *>(dev->d_fused), tr, pr, out, stream);
 }

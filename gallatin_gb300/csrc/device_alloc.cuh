@@ -31,4 +31,32 @@ struct gal_device_alloc {
   }
 };
 
+// Two allocators behind one malloc/free: the device arena first, the host
+// arena (GAL_FLAG_HOST_ARENA) when that returns NULL; free goes to the arena
+// that owns the pointer (the reference's global_malloc_fused /
+// global_free_fused, global_allocator.cuh:186-216). Lives in device memory so
+// that kernels templated on the allocator type take it like the others.
+struct gal_fused_device_alloc {
+  gal_device_alloc *dev;
+  gal_device_alloc *host;
+  __device__ __forceinline__ void *malloc_w(uint64_t n, uint32_t w) {
+    void *p = dev->malloc_w(n, w);
+    return p != nullptr ? p : host->malloc_w(n, w);
+  }
+  __device__ __forceinline__ void free_w(void *p, uint32_t w) {
+    if (dev->owns_allocation(p)) {
+      dev->free_w(p, w);
+    } else {
+      host->free_w(p, w);
+    }
+  }
+  __device__ __forceinline__ void *malloc(uint64_t n) { return malloc_w(n, 32); }
+  __device__ __forceinline__ void free(void *p) { free_w(p, 32); }
+  // segments both arenas hold, for fragmentation (both have the same segment size)
+  __device__ inline uint64_t owned_segments() const { return dev->owned_segments() + host->owned_segments(); }
+  __device__ inline uint64_t owned_segments_warp(uint32_t lane) const {
+    return dev->owned_segments_warp(lane) + host->owned_segments_warp(lane);
+  }
+};
+
 #endif  // GALLATIN_GB300_DEVICE_ALLOC_CUH

@@ -307,6 +307,16 @@ typedef struct gal_serve_out_t { /* device arrays, cleared by the call */
 int gal_run_serving(gal_allocator *h, const gal_serve_trace_t *trace, const gal_serve_params_t *params,
                     const gal_serve_out_t *out, void *stream);
 
+/* The same loop with every page malloc device-first: from `dev`, and from
+ * `host` (normally a GAL_FLAG_HOST_ARENA allocator of the same segment size)
+ * when that returns NULL; each free goes to the arena that owns the page (the
+ * reference's global_malloc_fused / global_free_fused,
+ * global_allocator.cuh:186-216). The page budget may then exceed the device
+ * arena: pages past it spill to host memory. step_stats owned segments count
+ * both arenas. Scratch is owned by `dev`. */
+int gal_run_serving_fused(gal_allocator *dev, gal_allocator *host, const gal_serve_trace_t *trace,
+                          const gal_serve_params_t *params, const gal_serve_out_t *out, void *stream);
+
 /* --- allocator-backed data structures (reference data_structs/
  *     chaining_table.cuh:57-327 and single_vector.cuh:50-200) ---
  * A chained hash table of u64 keys and values: buckets hold chains of 120 B

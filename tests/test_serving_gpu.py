@@ -94,3 +94,30 @@ def test_serving_rejects_bad_parameters(cuda):
             a.run_serving(ctypes.byref(run.c_trace), ctypes.byref(p), ctypes.byref(run.c_out))
         with pytest.raises(ValueError):
             ServingRun(cuda, tr, budget_pages=BUDGET, max_pages=4)
+
+
+def test_pages_spill_to_a_host_arena_with_the_same_results(cuda):
+    # the live pages peak near 226 MiB, well past the 64 MiB device arena:
+    # through the fused calls the pages that do not fit land in a host arena,
+    # no malloc fails, and every stream's admission, finish and checksum are
+    # those of a run on a device arena large enough for all of it
+    tr = small(8)
+    want = run_once(cuda, tr, True)
+    dev = gal.Gallatin.generate_on_device(64 << 20, 5, print_info=False)
+    host = gal.Gallatin.generate_on_device_host(1 << 30, 6, print_info=False)
+    try:
+        run = ServingRun(cuda, tr, budget_pages=BUDGET, max_slots=SLOTS)
+        run.run(lambda *a: dev.run_serving_fused(host, *a), persistent=True)
+        res = run.results()
+        assert res["step_stats"][:, 7].sum() == 0, "a page malloc returned NULL"
+        for k in ("checksum", "admit_step", "finish_step"):
+            assert np.array_equal(res[k], want[k]), k
+        assert host.stats()["counters"]["block_pins"] > 0, "nothing spilled to the host arena"
+        assert dev.stats()["counters"]["nomem"] > 0
+        for a in (dev, host):
+            a.flush_pinned()
+            cuda.cuda.synchronize()
+            check_restored(a)
+    finally:
+        dev.free_on_device()
+        host.free_on_device()
