@@ -83,6 +83,12 @@ WORKLOADS = {
     # the first and last u64) and a drain launch (verify, free)
     "spill": dict(arena=4 * GIB, host_arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096,
                   threads=8_388_608),
+    # the serving loop under memory pressure: the same trace and gate (80 % of
+    # all memory) over an 8 GiB device arena and a 16 GiB pinned host arena,
+    # every page malloc device-first with the host arena on NULL
+    "serving-spill": dict(arena=8 * GIB, host_arena=16 * GIB, segment=16 * MIB, min_size=16, max_size=4096,
+                          steps=600, arrivals=1000.0, page_bytes=8192, slots=262144, max_pages=2048, gate=0.8,
+                          ctas_per_sm=1),
     # the mixed-slices workload on an allocator that returns zeroed memory
     # (the reference's running_calloc): every free zeroes its slices
     "calloc": dict(
@@ -284,12 +290,12 @@ def cpu_baseline(name: str, w: dict) -> dict:
         return {"value": pushes / secs, "unit": "pushes/s", "cores": cores, "kind": "port", "seconds": secs,
                 "misses": bad,
                 "sample": f"full workload: {w['vectors']} vectors grown by doubling with glibc malloc/copy/free"}
-    elif name == "serving":
+    elif name in ("serving", "serving-spill"):
         from gallatin_gb300.serving import quantile_ns
         from gallatin_gb300.workload import serving_admission, serving_trace
 
         trace = serving_trace(42, steps=w["steps"], arrivals_per_step=w["arrivals"])
-        budget = int(w["gate"] * w["arena"]) // w["page_bytes"]
+        budget = int(w["gate"] * (w["arena"] + w.get("host_arena", 0))) // w["page_bytes"]
         admit, _ = serving_admission(trace, budget, w["slots"])
         secs, checksums, hist, misses = oracle.cpu_replay_serving(trace, admit, page_bytes=w["page_bytes"],
                                                                   workers=cores)
@@ -441,13 +447,15 @@ def run(args) -> dict | None:
 
         gal.load()
 
-    unit = {"batches": "requests/s", "serving": "pages/s", "table": "key ops/s", "vectors": "pushes/s"}.get(
+    serving = args.workload in ("serving", "serving-spill")
+    unit = {"batches": "requests/s", "serving": "pages/s", "serving-spill": "pages/s", "table": "key ops/s",
+            "vectors": "pushes/s"}.get(
         args.workload, "malloc+free pairs/s")
     stream = torch.cuda.current_stream()
     s_ptr = stream.cuda_stream
     a = make_allocator(impl, w)
     ha = None
-    if args.workload == "spill":
+    if args.workload in ("spill", "serving-spill"):
         try:
             ha = make_allocator(impl, w, host=True)
         except RuntimeError as e:
@@ -656,7 +664,7 @@ def run(args) -> dict | None:
             "max_size": w["max_size"], "vectors": len(lengths), "pushes": units, "seed": 42,
             "l2": "flushed (256 MiB write) before every timed step",
         }
-    elif args.workload == "serving":
+    elif serving:
         from gallatin_gb300.serving import ServingRun
         from gallatin_gb300.workload import serving_trace
 
@@ -665,7 +673,13 @@ def run(args) -> dict | None:
         elif impl == "reference":
             w["steps"] = REF_SERVE_STEPS
         trace = serving_trace(42, steps=w["steps"], arrivals_per_step=w["arrivals"])
-        budget = int(w["gate"] * w["arena"]) // w["page_bytes"]
+        budget = int(w["gate"] * (w["arena"] + w.get("host_arena", 0))) // w["page_bytes"]
+        if ha is not None:
+            # device first, the host arena when the device has no page
+            def entry(*x):
+                return a.run_serving_fused(ha, *x)
+        else:
+            entry = a.run_serving
         srv_kw = dict(budget_pages=budget, page_bytes=w["page_bytes"], max_slots=w["slots"], max_pages=w["max_pages"])
         srv = ServingRun(torch, trace, **srv_kw)
         persistent = impl != "reference"
@@ -673,11 +687,11 @@ def run(args) -> dict | None:
         geo = w["ctas_per_sm"] if persistent else 0
 
         def step():
-            srv.run(a.run_serving, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
+            srv.run(entry, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
 
         def e2e_step():
             r = ServingRun(torch, trace, **srv_kw)  # trace to the device
-            r.run(a.run_serving, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
+            r.run(entry, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
             res_e = r.results()  # outputs back to the host
             out = np.zeros(8, dtype=np.uint64)
             out[0] = res_e["step_stats"][:, 7].sum()
@@ -690,8 +704,11 @@ def run(args) -> dict | None:
         config = {
             "workload": f"serving: Poisson arrivals 2,000 streams/s, 0.5 s per step, {w['steps']} steps, "
                         "lognormal(ln 1024, 1.0) tokens in [128, 32768], one 8 KiB page (16 tokens) per step per "
-                        "stream, pages freed at completion, admission gated at 80 % of the arena",
-            "arena_bytes": w["arena"], "segment_bytes": w["segment"], "min_size": w["min_size"],
+                        "stream, pages freed at completion, admission gated at 80 % of the arena" + (
+                            "s (device and pinned host); pages device-first, host arena on NULL" if ha is not None
+                            else ""),
+            "arena_bytes": w["arena"], "host_arena_bytes": w.get("host_arena", 0), "segment_bytes": w["segment"],
+            "min_size": w["min_size"],
             "max_size": w["max_size"], "steps": w["steps"], "streams": n_str, "budget_pages": budget,
             "slots": w["slots"], "seed": 42,
             "path": ("reference: plain path, one launch per phase per step" if impl == "reference"
@@ -718,7 +735,7 @@ def run(args) -> dict | None:
         step()
     torch.cuda.synchronize()
     stats.zero_()
-    if args.workload == "serving":
+    if serving:
         units = int(srv.results()["step_stats"][:, 0].sum())
         alg_bytes = units * 256  # 16 tokens written into each page and read back
 
@@ -761,7 +778,7 @@ def run(args) -> dict | None:
             "value": replica_throughput(units, args.steps, world, e2e_total * 1e3),
             "unit": unit,
             "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h if args.workload == "serving" else 64,
+            "d2h_bytes_per_step": d2h if serving else 64,
             "ms_per_step": 1e3 * e2e_total / args.steps,
             "misses": int(e2e_bad[0]),
             "verify_failures": int(e2e_bad[1]),
@@ -790,6 +807,8 @@ def run(args) -> dict | None:
     result = {
         "metric": {"batches": "malloc+free ops/s (one op = one malloc or one free request)",
                    "serving": "page allocations/s of the serving loop (p50/p99 page-malloc latency in 'serving')",
+                   "serving-spill": "page allocations/s of the serving loop over device + host arenas (p50/p99 "
+                                    "page-malloc latency in 'serving')",
                    "table": "chained hash table key ops/s (insert + erase + reinsert, nodes from the allocator)",
                    "vectors": "vector push_back/s (doubling backings from the allocator)",
                    }.get(args.workload, "malloc+free ops/s (one op = one malloc + its free)"),
@@ -827,7 +846,7 @@ def run(args) -> dict | None:
     if args.workload == "vectors":
         result["verify_failures"] = int(st[2])
         result["checks"] = {"pushes": int(st[4]), "expected_pushes": units * args.steps}
-    if args.workload == "serving":
+    if serving:
         from gallatin_gb300.serving import summarize
         from gallatin_gb300.workload import serving_admission
 
@@ -836,7 +855,7 @@ def run(args) -> dict | None:
                                       seconds=ms_per_step / 1e3)
         admit_model, _ = serving_admission(trace, budget, w["slots"])
         result["serving"]["admission_matches_model"] = bool(np.array_equal(res["admit_step"], admit_model))
-        if impl == "gb300" and not args.no_prefix:
+        if impl == "gb300" and not args.no_prefix and ha is None:
             # the plain path (one launch per phase per step) on the same trace
             srv0 = ServingRun(torch, trace, **srv_kw)
             srv0.run(a.run_serving, persistent=False, stream=s_ptr)
@@ -855,17 +874,18 @@ def run(args) -> dict | None:
             plain["same_results"] = bool(np.array_equal(res0["checksum"], res["checksum"]) and
                                          np.array_equal(res0["admit_step"], res["admit_step"]))
             result["serving"]["plain_path"] = plain
+        if impl == "gb300" and not args.no_prefix:
             # the device loop on the reference arm's sample (its first steps)
             if w["steps"] != REF_SERVE_STEPS:
                 tr_s = serving_trace(42, steps=REF_SERVE_STEPS, arrivals_per_step=w["arrivals"])
                 srv_s = ServingRun(torch, tr_s, **srv_kw)
-                srv_s.run(a.run_serving, persistent=True, ctas_per_sm=geo, stream=s_ptr)
+                srv_s.run(entry, persistent=True, ctas_per_sm=geo, stream=s_ptr)
                 torch.cuda.synchronize()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 flush.fill_(1)
                 e0.record(stream)
-                srv_s.run(a.run_serving, persistent=True, ctas_per_sm=geo, stream=s_ptr)
+                srv_s.run(entry, persistent=True, ctas_per_sm=geo, stream=s_ptr)
                 e1.record(stream)
                 e1.synchronize()
                 ms_s = e0.elapsed_time(e1)
@@ -886,6 +906,7 @@ def run(args) -> dict | None:
             result_autotune = autotune_batches(reqs, offsets, slots, arena=w["arena"])
     if args.workload == "spill":
         result["spill"] = {"host_served": int(st[4]), "host_fraction": int(st[4]) / max(units * args.steps, 1)}
+    if ha is not None:
         close_allocator(impl, ha)
     if impl == "gb300" and a is not None:
         st_all = a.stats()
@@ -897,7 +918,7 @@ def run(args) -> dict | None:
         result["autotune"] = result_autotune
     if rank == 0 and impl == "gb300" and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(args.workload, w)
-        if args.workload == "serving":
+        if serving:
             # the glibc replay computes every finished stream's checksum on the
             # host: the device must report the same ones
             want = result["cpu_baseline"].pop("_checksums")

@@ -12,6 +12,8 @@ struct gal_device_alloc {
   __device__ __forceinline__ void *malloc_w(uint64_t n, uint32_t w) { return gal::malloc(&state, n, w); }
   __device__ __forceinline__ void free_w(void *p, uint32_t w) { gal::free(&state, p, w); }
   __device__ __forceinline__ bool owns_allocation(const void *p) const { return gal::owns_allocation(&state, p); }
+  // NULL at once for a slice class known to have no room (see gal::malloc_unless_full)
+  __device__ __forceinline__ void *malloc_first_w(uint64_t n, uint32_t w) { return gal::malloc_unless_full(&state, n, w); }
   // segments not in the segment tree (formatted for a tree or part of a
   // multi-segment allocation): a snapshot, read while others may change it
   __device__ inline uint64_t owned_segments() const {
@@ -40,7 +42,7 @@ struct gal_fused_device_alloc {
   gal_device_alloc *dev;
   gal_device_alloc *host;
   __device__ __forceinline__ void *malloc_w(uint64_t n, uint32_t w) {
-    void *p = dev->malloc_w(n, w);
+    void *p = dev->malloc_first_w(n, w);
     return p != nullptr ? p : host->malloc_w(n, w);
   }
   __device__ __forceinline__ void free_w(void *p, uint32_t w) {

@@ -30,6 +30,17 @@ namespace galwork {
 
 enum { STAT_HOST = 4 };  // fill: allocations served by the host arena
 
+// The device attempt of the pair: an allocator that can tell at once that a
+// request's class has no room (malloc_first_w) skips the search.
+template <class A>
+__device__ __forceinline__ auto first_attempt(A *a, uint64_t n, int) -> decltype(a->malloc_first_w(n, 32u)) {
+  return a->malloc_first_w(n, 32u);
+}
+template <class A>
+__device__ __forceinline__ void *first_attempt(A *a, uint64_t n, long) {
+  return a->malloc(n);
+}
+
 // Device-first allocation with a host-arena fallback over two allocators of
 // one type: malloc from `dev`, and from `host` when that returns NULL; free
 // to whichever arena holds the pointer. The reference's global_malloc_fused
@@ -41,9 +52,9 @@ struct fused_alloc {
   A *host;  // NULL: the device arena alone
 
   __device__ __forceinline__ void *malloc(uint64_t n) const {
-    void *p = dev->malloc(n);
-    if (p == nullptr && host != nullptr) p = host->malloc(n);
-    return p;
+    if (host == nullptr) return dev->malloc(n);
+    void *p = first_attempt(dev, n, 0);
+    return p != nullptr ? p : host->malloc(n);
   }
   __device__ __forceinline__ void free(void *p) const {
     if (host == nullptr || dev->owns_allocation(p)) {

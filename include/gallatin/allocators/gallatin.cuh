@@ -97,6 +97,11 @@ struct Gallatin {
 
   __device__ void free(void *allocation) { gal::free(&state, allocation); }
 
+  // malloc that returns NULL at once for a slice class whose last block
+  // replacement found the arena out of blocks (no reference counterpart;
+  // the fused calls use it before falling back to host memory)
+  __device__ void *malloc_unless_full(uint64_t size) { return gal::malloc_unless_full(&state, size); }
+
   __device__ uint64_t get_allocated_size(uint64_t bytes_needed) { return gal::allocated_size(&state, bytes_needed); }
 
   __device__ bool owns_allocation(void *alloc) { return gal::owns_allocation(&state, alloc); }

@@ -107,7 +107,8 @@ __device__ inline void global_free_combined(void *ptr, bool on_host = false) {
 //      were placed until freed ----
 
 __device__ inline void *global_malloc_fused(uint64_t num_bytes) {
-  void *alloc = global_malloc(num_bytes);
+  // a class the device arena is known to be out of goes straight to the host
+  void *alloc = global_gallatin->malloc_unless_full(num_bytes);
   return alloc != nullptr ? alloc : global_malloc_host(num_bytes);
 }
 

@@ -290,6 +290,12 @@ __device__ inline uint32_t take_block(const gal_state_t *st, uint64_t seg, uint3
   return GAL_EMPTY_BLOCK;
 }
 
+// A block or segment went back to its pool: the no-memory hints of every
+// class are out of date.
+__device__ __forceinline__ void clear_nomem(const gal_state_t *st) {
+  if (ptx::ld_relaxed(st->nomem)) atomicExch(st->nomem, 0u);
+}
+
 // Give a retired block back to its segment's free-block bitmap.
 __device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b) {
   const int bis = block_index_shift(st);
@@ -298,6 +304,7 @@ __device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b
   ptx::red_or_relaxed(st->seg_block_bits + seg * st->seg_block_words + (i >> 6), 1ull << (i & 63));
   seg_avail_add_one(st, seg);  // release add orders the bit before the count
   count(st, GAL_CTR_BLOCK_RETIRE);
+  clear_nomem(st);
 }
 
 // A block belongs in class k's adoptable tree exactly while it is DETACHED
@@ -859,6 +866,7 @@ __device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_
   }
   __threadfence();
   veb::return_run(&st->segment_tree, seg, n);
+  clear_nomem(st);
 }
 
 // ---- zeroing for GAL_FLAG_CALLOC ------------------------------------------
@@ -942,6 +950,20 @@ __device__ inline void free(const gal_state_t *st, void *ptr, uint32_t width = 3
   } else {
     count(st, GAL_CTR_BAD_FREE);
   }
+}
+
+// malloc, except that a slice request of a class whose last slot
+// replacement found no block (and no block or segment has gone back to a
+// pool since) returns NULL at once: for callers with somewhere else to go,
+// such as the device-first / host-arena pair, which would otherwise pay for
+// a search that is known to fail.
+__device__ __forceinline__ void *malloc_unless_full(const gal_state_t *st, uint64_t size, uint32_t width = 32) {
+  const size_class sc = classify(st, size);
+  if (sc.tier == TIER_SLICE) {
+    const uint32_t k = sc.tree + (uint32_t)(__ffs((int)sc.count) - 1);
+    if ((ptx::ld_relaxed(st->nomem) >> k) & 1u) return nullptr;
+  }
+  return malloc(st, size, width);
 }
 
 // Bytes a request of `size` really occupies (reference get_allocated_size,

@@ -245,6 +245,7 @@ def _bind_ref(lib):
         "galref_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "galref_run_batches": (i32, [vp, vp, vp, vp, u32, vp, u32, vp, vp]),
         "galref_run_serving": (i32, [vp, vp, vp, vp, vp]),
+        "galref_run_serving_fused": (i32, [vp, vp, vp, vp, vp, vp]),
         "galref_table_op": (i32, [vp, vp, u64, u64, u32, vp, u64, u64, vp, vp]),
         "galref_run_vectors": (i32, [vp, vp, u64, u32, vp, vp]),
     }
@@ -337,6 +338,11 @@ class RefGallatin:
         """The serving loop's plain path (one launch per phase per step) over
         the reference allocator; the params' mode is ignored."""
         return self._lib.galref_run_serving(self._h, trace_ptr, params_ptr, out_ptr, stream)
+
+    def run_serving_fused(self, host, trace_ptr, params_ptr, out_ptr, stream=0):
+        """The plain-path serving loop over this allocator first and `host`
+        (a host-arena RefGallatin) when it returns NULL; default geometry only."""
+        return self._lib.galref_run_serving_fused(self._h, host._h, trace_ptr, params_ptr, out_ptr, stream)
 
     def table_op(self, heads_ptr, nbuckets, seed, op, n, d_stats, *, d_keys=None, key_seed=42, stream=0):
         """The chained table of gallatin_gb300/structures.cuh over the reference allocator."""

@@ -83,6 +83,7 @@ struct RefAlloc {
   unsigned long long *d_stats;
   void *d_serve;
   uint64_t d_serve_bytes;
+  void *d_fused;  // device copy of the fused pair for the fused serving loop
 };
 
 int config_of(uint64_t seg, uint64_t mn, uint64_t mx) {
@@ -238,6 +239,35 @@ int galref_run_serving(void *h, const gal_serve_trace_t *tr, const gal_serve_par
   }
 }
 
+// The serving loop with every page malloc device-first over two reference
+// allocators (the second from generate_on_device_host): the reference's
+// global_malloc_fused / global_free_fused pattern (global_allocator.cuh:
+// 186-216) through galwork::fused_alloc. Default geometry only.
+int galref_run_serving_fused(void *dev_h, void *host_h, const gal_serve_trace_t *tr, const gal_serve_params_t *pr,
+                             const gal_serve_out_t *out, void *stream) {
+  RefAlloc *a = (RefAlloc *)dev_h;
+  RefAlloc *b = (RefAlloc *)host_h;
+  if (a->config != 0 || b->config != 0) return 1;
+  const galserve::layout_t l = galserve::layout(pr->max_slots, pr->max_pages);
+  if (l.total > a->d_serve_bytes) {
+    if (a->d_serve) cudaFree(a->d_serve);
+    a->d_serve = nullptr;
+    a->d_serve_bytes = 0;
+    if (cudaMalloc(&a->d_serve, l.total) != cudaSuccess) return 3;
+    a->d_serve_bytes = l.total;
+  }
+  using fused = galwork::fused_alloc<ref_16m_16_4096>;
+  if (a->d_fused == nullptr && cudaMalloc(&a->d_fused, sizeof(fused)) != cudaSuccess) return 3;
+  const fused f{(ref_16m_16_4096 *)a->dev, (ref_16m_16_4096 *)b->dev};
+  if (cudaMemcpy(a->d_fused, &f, sizeof(f), cudaMemcpyHostToDevice) != cudaSuccess) return 2;
+  const galserve::server_t sv = galserve::server_at(a->d_serve, pr->max_slots, pr->max_pages);
+  galserve::trace_t t{tr->n_streams, tr->arrivals_end, tr->tokens, tr->pages, tr->page_prefix, tr->ids};
+  galserve::params_t p{pr->steps, pr->tokens_per_page, pr->page_bytes, pr->budget_pages, pr->seed, 32};
+  galserve::out_t o{out->checksum, out->admit_step, out->finish_step, out->step_stats,
+                    (unsigned long long *)out->latency_hist};
+  return launch_serving<fused>(a->d_fused, sv, t, p, o, (cudaStream_t)stream);
+}
+
 int galref_run_batches(void *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,
                        uint32_t n_batches, uint64_t *d_table, uint32_t mode, unsigned long long *d_stats,
                        void *stream) {
@@ -303,6 +333,7 @@ int galref_create(uint64_t max_bytes, uint64_t seed, uint64_t seg, uint64_t mn, 
   a->d_classes_bytes = 0;
   a->d_serve = nullptr;
   a->d_serve_bytes = 0;
+  a->d_fused = nullptr;
   switch (config) {
     case 0: a->dev = ref_16m_16_4096::generate_on_device(max_bytes, seed, false); break;
     case 1: a->dev = ref_16m_128_4096::generate_on_device(max_bytes, seed, false); break;
@@ -332,6 +363,7 @@ int galref_create_host(uint64_t max_bytes, uint64_t seed, uint64_t seg, uint64_t
   a->d_classes_bytes = 0;
   a->d_serve = nullptr;
   a->d_serve_bytes = 0;
+  a->d_fused = nullptr;
   switch (config) {
     case 0: a->dev = ref_16m_16_4096::generate_on_device_host(max_bytes, seed, false); break;
     case 1: a->dev = ref_16m_128_4096::generate_on_device_host(max_bytes, seed, false); break;
@@ -374,6 +406,7 @@ int galref_destroy(void *h) {
   }
   if (a->d_classes) cudaFree(a->d_classes);
   if (a->d_serve) cudaFree(a->d_serve);
+  if (a->d_fused) cudaFree(a->d_fused);
   cudaFree(a->d_stats);
   delete a;
   return 0;
