@@ -102,9 +102,18 @@ def test_one_class_packs_blocks(cuda):
         release_all(cuda, a, ptrs)
 
 
-def test_slice_tier_fills_to_capacity_then_returns_null(cuda):
+def make_arena(nbytes, seed, host):
+    """A device-arena allocator, or the same over pinned host memory (the
+    reference's generate_on_device_host; its tests fill it to capacity the
+    same way, tests/src/gallatin_host_test.cu:136-200)."""
+    make = gal.Gallatin.generate_on_device_host if host else gal.Gallatin.generate_on_device
+    return make(nbytes, seed, print_info=False)
+
+
+@pytest.mark.parametrize("host", [False, True], ids=["device-arena", "host-arena"])
+def test_slice_tier_fills_to_capacity_then_returns_null(cuda, host):
     # 4 segments of 16 MiB; a 4 KiB block is a whole segment: 4 * 4096 slices
-    with gal.Gallatin.generate_on_device(64 << 20, 3, print_info=False) as a:
+    with make_arena(64 << 20, 3, host) as a:
         cap = 4 * 4096
         sizes = np.full(cap + 100, 4096, dtype=np.uint64)
         ptrs = malloc_batch(cuda, a, sizes)
@@ -114,8 +123,9 @@ def test_slice_tier_fills_to_capacity_then_returns_null(cuda):
         release_all(cuda, a, ptrs)
 
 
-def test_block_and_segment_tiers_exact_capacity(cuda):
-    with gal.Gallatin.generate_on_device(64 << 20, 4, print_info=False) as a:
+@pytest.mark.parametrize("host", [False, True], ids=["device-arena", "host-arena"])
+def test_block_and_segment_tiers_exact_capacity(cuda, host):
+    with make_arena(64 << 20, 4, host) as a:
         ptrs = malloc_batch(cuda, a, np.full(5, 16 << 20, dtype=np.uint64))  # whole-segment blocks
         assert int((ptrs != 0).sum()) == 4
         free_batch(cuda, a, ptrs)
