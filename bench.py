@@ -552,6 +552,7 @@ def run(args) -> dict | None:
                 a.run_batches(*bargs, persistent=False, stream=s_ptr)
 
             e2e_step = None
+            launches_per_step = int(np.count_nonzero(np.diff(offsets)))  # one per non-empty batch
         else:
             graph = a.capture_batches(*bargs, width=w["width"], persistent=True, binned=w["binned"])
 
@@ -602,6 +603,8 @@ def run(args) -> dict | None:
 
         def step():
             run_ops(ops)
+
+        launches_per_step = len(ops)  # one kernel per table operation
 
         with np.errstate(over="ignore"):
             h_keys = torch.from_numpy(splitmix64(np.arange(n, dtype=np.uint64) + np.uint64(42)).view(np.int64))
@@ -685,6 +688,10 @@ def run(args) -> dict | None:
         persistent = impl != "reference"
 
         geo = w["ctas_per_sm"] if persistent else 0
+        # the loop's own kernels per run: two init kernels, then one
+        # cooperative launch (device loop) or a prologue, two per step and a
+        # drain (plain path)
+        launches_per_step = 3 if persistent else 2 + 1 + 2 * w["steps"] + 1
 
         def step():
             srv.run(entry, persistent=persistent, ctas_per_sm=geo, stream=s_ptr)
