@@ -73,6 +73,8 @@ extern "C" int gal_run_serving_fused(gal_allocator *dev, gal_allocator *host, co
   if (dev->d_fused == nullptr) GAL_CUDA_TRY(cudaMalloc(&dev->d_fused, sizeof(gal_fused_device_alloc)), "cudaMalloc fused");
   const gal_fused_device_alloc f{reinterpret_cast<gal_device_alloc *>(dev->d_state),
                                  reinterpret_cast<gal_device_alloc *>(host->d_state)};
-  GAL_CUDA_TRY(cudaMemcpy(dev->d_fused, &f, sizeof(f), cudaMemcpyHostToDevice), "fused pair H2D");
+  // ordered on the run's stream, after any earlier run that still reads the pair
+  GAL_CUDA_TRY(cudaMemcpyAsync(dev->d_fused, &f, sizeof(f), cudaMemcpyHostToDevice, (cudaStream_t)stream),
+               "fused pair H2D");
   return run_serving_on(dev, reinterpret_cast<gal_fused_device_alloc *>(dev->d_fused), tr, pr, out, stream);
 }
