@@ -585,7 +585,10 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     const uint32_t g_n = __popc(grp);
     const uint32_t g_rank = __popc(grp & lt);
     const uint32_t need = g_n * c;
-    uint64_t *const slot = slots + (slot0 + (uint32_t)(attempt >> 3) + strikes + hops) % nslots;
+    // after a miss each slot is visited once, in order from slot0 + 1, so a
+    // strike on every slot means every slot was seen full or empty
+    uint64_t *const slot =
+        slots + (strikes ? (slot0 + strikes) % nslots : (slot0 + (uint32_t)(attempt >> 3) + hops) % nslots);
 
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;

@@ -142,11 +142,12 @@ int main() {
   cudaError_t e4 = cudaDeviceSynchronize();
   my_alloc::free_on_device(za);
   using host_alloc = Gallatin<16ull * 1024 * 1024, 16ull, 4096ull>;
-  host_alloc *ha = host_alloc::generate_on_device_host(64ull << 20, 10, false, true);
-  calloc_rounds<host_alloc><<<16, 256>>>(ha, 4096, 4, dirty + 1);
+  // 16 segments: every size class of the rounds below gets segments of its own
+  host_alloc *ha = host_alloc::generate_on_device_host(256ull << 20, 10, false, true);
   uint64_t **hp = nullptr;
   cudaMallocManaged(&hp, sizeof(uint64_t *));
   host_arena_write<host_alloc><<<1, 1>>>(ha, hp);
+  calloc_rounds<host_alloc><<<16, 256>>>(ha, 4096, 4, dirty + 1);
   cudaError_t e5 = cudaDeviceSynchronize();
   // the host arena is host memory: the CPU reads what the kernel wrote
   bool host_read_ok = *hp != nullptr;
