@@ -41,6 +41,34 @@ __global__ void typed_churn(Alloc *alloc, uint64_t n, unsigned long long *errors
   alloc->free(p);
 }
 
+// reference tests/src/gallatin_single_thread.cu shape: one thread mallocs
+// n allocations in sequence, then checks and frees them in sequence
+__global__ void single_thread_alloc(uint64_t n, uint64_t **table, unsigned long long *counts) {
+  if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint64_t size = 16ull << (i % 9);
+    uint64_t *p = (uint64_t *)global_malloc(size);
+    table[i] = p;
+    if (p == nullptr) {
+      counts[0] += 1;
+      continue;
+    }
+    p[0] = i;
+    p[size / 8 - 1] = ~i;
+  }
+}
+
+__global__ void single_thread_free(uint64_t n, uint64_t **table, unsigned long long *counts) {
+  if (threadIdx.x + blockIdx.x * blockDim.x != 0) return;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t *p = table[i];
+    if (p == nullptr) continue;
+    const uint64_t size = 16ull << (i % 9);
+    if (p[0] != i || p[size / 8 - 1] != ~i) counts[1] += 1;
+    global_free(p);
+  }
+}
+
 // reference tests/src/global_exceed_test.cu shape: insert through the fused
 // call, then verify and free through the fused call
 __global__ void fused_fill(uint64_t n, uint64_t **table, unsigned long long *counts) {
@@ -100,8 +128,20 @@ int main() {
   init_global_allocator(1ull << 30, 111, false);
   global_churn<<<(1 << 18) / 256, 256>>>(1 << 18, 4, errors);
   cudaError_t e = cudaDeviceSynchronize();
+  // one thread, 4,000 allocations in sequence, then their check and free
+  uint64_t **st_table = nullptr;
+  unsigned long long *st_counts = nullptr;
+  cudaMalloc(&st_table, 4000 * sizeof(uint64_t *));
+  cudaMallocManaged(&st_counts, 2 * sizeof(unsigned long long));
+  st_counts[0] = st_counts[1] = 0;
+  single_thread_alloc<<<1, 1>>>(4000, st_table, st_counts);
+  single_thread_free<<<1, 1>>>(4000, st_table, st_counts);
+  cudaError_t e_st = cudaDeviceSynchronize();
+  cudaFree(st_table);
   print_global_stats();
   free_global_allocator();
+  printf("single thread: misses %llu verify %llu; cuda %s\n", st_counts[0], st_counts[1], cudaGetErrorString(e_st));
+  const bool single_ok = e_st == cudaSuccess && st_counts[0] == 0 && st_counts[1] == 0;
 
   using my_alloc = Gallatin<16ull * 1024 * 1024, 128ull, 4096ull>;
   my_alloc *alloc = my_alloc::generate_on_device(512ull << 20, 7, false);
@@ -160,7 +200,7 @@ int main() {
   printf("errors: global misses %llu verify %llu; typed misses %llu checks %llu; cuda %s %s\n", errors[0], errors[1],
          errors[2], errors[3], cudaGetErrorString(e), cudaGetErrorString(e2));
   const bool ok = e == cudaSuccess && e2 == cudaSuccess && errors[0] == 0 && errors[1] == 0 && errors[2] == 0 &&
-                  errors[3] == 0 && fused_ok && calloc_ok;
+                  errors[3] == 0 && fused_ok && calloc_ok && single_ok;
   printf(ok ? "DROPIN OK\n" : "DROPIN FAILED\n");
   return ok ? 0 : 1;
 }
