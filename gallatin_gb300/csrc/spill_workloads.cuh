@@ -3,7 +3,7 @@
 //
 // The fused fill/drain templates are instantiated over the GB300 allocator
 // (capi_spill.cu) and over the reference's Gallatin<...>
-// (oracle/ref_harness.cu), so both sides of the comparison run the same
+// (the oracle/ref_*.cu harness), so both sides of the comparison run the same
 // kernels.
 //
 //   fill   thread i: malloc 16 << class_i bytes through fused_alloc, keep the

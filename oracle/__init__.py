@@ -2,7 +2,7 @@
 
 Bindings to the CPU restatement of the reference vEB tree (veb_oracle.c), the
 glibc CPU-baseline replay (cpu_replay.c) and, when it has been built, the
-reference's own CUDA build (oracle/_ref/libgalref.so, from ref_harness.cu).
+reference's own CUDA build (oracle/_ref/libgalref_*.so, from the oracle/ref_*.cu harness).
 Only tests/, the smoke check and bench.py's baseline legs use this package;
 the product (gallatin_gb300/) never imports it.
 """
@@ -206,28 +206,35 @@ def cpu_replay_pairs(n, size, workers=1):
 
 # -- the reference's own CUDA build -------------------------------------------
 def load_ref(build_if_missing: bool = True):
-    """ctypes handle of oracle/_ref/libgalref.so, or None when unavailable."""
+    """The reference harness's entry points (oracle/_ref/libgalref_*.so) as
+    attributes of one object, or None when unavailable."""
     global _REF
     if _REF is not None:
         return _REF
     import os
 
-    override = os.environ.get("GALLATIN_REF_LIB")
+    if os.environ.get("GALLATIN_SKIP_REF"):
+        return None  # runs that do not need the reference skip its long build
+    override = os.environ.get("GALLATIN_REF_LIB")  # os.pathsep-separated libraries
     if override:
-        _REF = _bind_ref(ctypes.CDLL(override))
+        _REF = _bind_ref([ctypes.CDLL(p) for p in override.split(os.pathsep) if p])
         return _REF
-    if build_if_missing and not build.ref_lib().exists():
+    if build_if_missing and not all(p.exists() for p in build.ref_libs()):
         try:
             build.build_reference()
         except RuntimeError:
             return None
-    if not build.ref_lib().exists():
+    if not all(p.exists() for p in build.ref_libs()):
         return None
-    _REF = _bind_ref(ctypes.CDLL(str(build.ref_lib())))
+    _REF = _bind_ref([ctypes.CDLL(str(p)) for p in build.ref_libs()])
     return _REF
 
 
-def _bind_ref(lib):
+class _RefEntryPoints:
+    """Entry points gathered from the harness's family libraries."""
+
+
+def _bind_ref(libs):
     vp, u64, u32, i32 = c_void_p, c_uint64, c_uint32, c_int
     sigs = {
         "galref_veb_create": (i32, [u64, u64, POINTER(vp)]),
@@ -249,11 +256,21 @@ def _bind_ref(lib):
         "galref_table_op": (i32, [vp, vp, u64, u64, u32, vp, u64, u64, vp, vp]),
         "galref_run_vectors": (i32, [vp, vp, u64, u32, vp, vp]),
     }
+    out = _RefEntryPoints()
     for name, (res, args) in sigs.items():
-        fn = getattr(lib, name)
+        fn = None
+        for lib in libs:
+            try:
+                fn = getattr(lib, name)
+                break
+            except AttributeError:
+                continue
+        if fn is None:
+            raise RuntimeError(f"reference harness entry point {name} not found")
         fn.restype = res
         fn.argtypes = args
-    return lib
+        setattr(out, name, fn)
+    return out
 
 
 class RefVeb:

@@ -7,11 +7,16 @@
                                   unmodified from the reference checkout (an
                                   install step: the reference is header-only
                                   CUDA, and the GPU machine has no checkout)
-* oracle/_ref/libgalref.so        ref_harness.cu compiled with nvcc against
-                                  those headers
+* oracle/_ref/libgalref_<family>.so
+                                  the harness (ref_core.cu, ref_batches.cu,
+                                  ref_serving.cu, ref_ds.cu, ref_fused.cu)
+                                  compiled with nvcc against those headers,
+                                  one library per family so they build in
+                                  parallel
 
 Everything lands in git-ignored folders. The GPU machine rebuilds from the staged
-headers, since binaries built on this x86 host do not run there.
+headers, since binaries built on this x86 host do not run there. The
+reference checkout is read from $GALLATIN_REFERENCE, else /root/reference.
 """
 from __future__ import annotations
 
@@ -26,7 +31,8 @@ REPO_DIR = ORACLE_DIR.parent
 BUILD_DIR = ORACLE_DIR / "_build"
 REF_DIR = ORACLE_DIR / "_ref"
 REF_INCLUDE = REF_DIR / "include"
-REFERENCE_CHECKOUT = Path("/root/reference")
+REFERENCE_CHECKOUT = Path(os.environ.get("GALLATIN_REFERENCE", "/root/reference"))
+REF_FAMILIES = ["core", "batches", "serving", "ds", "fused"]
 # the hot path: the allocator and everything it includes
 REF_HEADERS = [
     "alloc_utils.cuh",
@@ -62,8 +68,12 @@ def replay_lib() -> Path:
     return BUILD_DIR / "libcpu_replay.so"
 
 
-def ref_lib() -> Path:
-    return REF_DIR / "libgalref.so"
+def ref_lib(family: str = "core") -> Path:
+    return REF_DIR / f"libgalref_{family}.so"
+
+
+def ref_libs() -> list[Path]:
+    return [ref_lib(f) for f in REF_FAMILIES]
 
 
 def build_oracle(force: bool = False) -> None:
@@ -96,39 +106,43 @@ def stage_reference() -> bool:
 
 
 def build_reference(force: bool = False) -> bool:
-    """Build oracle/_ref/libgalref.so if the reference headers are available."""
+    """Build oracle/_ref/libgalref_<family>.so if the reference headers are available."""
     if not stage_reference():
         return False
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not Path(nvcc).exists():
         return False
-    src = ORACLE_DIR / "ref_harness.cu"
-    deps = [src, *(REPO_DIR / "gallatin_gb300" / "csrc").glob("*.cuh")]
-    deps += list((REF_INCLUDE / "gallatin" / "allocators").glob("*.cuh"))
-    if not force and not _stale(ref_lib(), deps):
-        return True
-    cmd = [
-        nvcc,
-        "-std=c++17",
-        "-O3",
-        "-lineinfo",
-        "-gencode",
-        "arch=compute_103a,code=sm_103a",
-        "-Xcompiler",
-        "-fPIC",
-        "-shared",
-        "-w",
-        "-I",
-        str(REF_INCLUDE),
-        "-I",
-        str(REPO_DIR / "include"),
-        "-I",
-        str(REPO_DIR / "gallatin_gb300" / "csrc"),
-        str(src),
-        "-o",
-        str(ref_lib()),
-    ]
-    _run(cmd)
+    common = [ORACLE_DIR / "ref_common.cuh", *(REPO_DIR / "gallatin_gb300" / "csrc").glob("*.cuh")]
+    common += list((REF_INCLUDE / "gallatin" / "allocators").glob("*.cuh"))
+    common += list((REPO_DIR / "include").rglob("*.cuh")) + list((REPO_DIR / "include").rglob("*.h"))
+    cmds = []
+    for family in REF_FAMILIES:
+        src = ORACLE_DIR / f"ref_{family}.cu"
+        if not force and not _stale(ref_lib(family), [src, *common]):
+            continue
+        cmds.append([
+            nvcc,
+            "-std=c++17",
+            "-O3",
+            "-lineinfo",
+            "-gencode",
+            "arch=compute_103a,code=sm_103a",
+            "-Xcompiler",
+            "-fPIC",
+            "-shared",
+            "-w",
+            "-I",
+            str(REF_INCLUDE),
+            "-I",
+            str(REPO_DIR / "include"),
+            "-I",
+            str(REPO_DIR / "gallatin_gb300" / "csrc"),
+            str(src),
+            "-o",
+            str(ref_lib(family)),
+        ])
+    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
+        list(ex.map(_run, cmds))
     return True
 
 

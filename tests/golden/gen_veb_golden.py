@@ -3,8 +3,8 @@
 
 Seeded, ordered op sequences are run through the reference's own veb_tree
 (saltsystemslab/gallatin include/gallatin/allocators/veb.cuh, compiled
-unmodified into oracle/_ref/libgalref.so by oracle/build.py) with the
-single-block op runner of oracle/ref_harness.cu: op i executes on thread
+unmodified into oracle/_ref/libgalref_core.so by oracle/build.py) with the
+single-block op runner of oracle/ref_core.cu: op i executes on thread
 ops[i].tid, so the hashed ops (find_random_valid_index, malloc) see that
 thread id. The fixture stores, per sequence, the ops, every op's result and
 the final bit layers. Needs a GPU, torch and the staged reference headers.
