@@ -108,6 +108,40 @@ def measured_peaks() -> dict:
     return {}
 
 
+def l2_atomic_roofline(torch, stream, atomics_per_unit, units_per_s) -> dict:
+    """Peak L2 atomic rate of this GPU, measured here with the library's probe
+    (single-lane 64-bit atomics, each to its own 128-byte line, 8 in flight per
+    warp: the allocator's leader pattern), best of several launches timed with
+    CUDA events; and the allocator's achieved rate, atomics_per_unit (an ncu
+    count of L2 atomic + reduction requests of the timed kernel, per unit) x
+    units per second."""
+    import gallatin_gb300 as gal
+
+    buf = torch.zeros(32 * MIB, dtype=torch.uint8, device="cuda")
+    best = {}
+    for mode, name in ((0, "atom"), (1, "red")):
+        for ctas in (4, 8):
+            gal.probe_l2_atomics(buf.data_ptr(), buf.numel(), 64, mode, ctas, stream=stream.cuda_stream)  # warm-up
+            for _ in range(3):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                ops = gal.probe_l2_atomics(buf.data_ptr(), buf.numel(), 512, mode, ctas, stream=stream.cuda_stream)
+                e1.record(stream)
+                e1.synchronize()
+                rate = ops / (e0.elapsed_time(e1) / 1e3)
+                best[name] = max(best.get(name, 0.0), rate)
+    del buf
+    out = {"unit": "atomics/s", "peak": best["atom"], "peak_red": best["red"],
+           "peak_source": "measured in this run: gal_probe_l2_atomics, single-lane atom.add.u64 to distinct "
+                          "128-B lines, best of 3 launches x {4, 8} CTAs/SM",
+           "atomics_per_unit": atomics_per_unit, "achieved": None, "frac": None}
+    if atomics_per_unit:
+        out["achieved"] = atomics_per_unit * units_per_s
+        out["frac"] = out["achieved"] / out["peak"]
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle-reason samples during the timed region.
 
@@ -805,11 +839,23 @@ def run(args) -> dict | None:
         "algorithmic_bytes_per_launch": alg_bytes,
     }
     traffic_file = REPO / "profiles" / f"traffic_{impl}_{args.workload}.json"
+    traffic = {}
     if traffic_file.exists():
         try:
-            roofline["traffic"] = json.loads(traffic_file.read_text()).get("dram_bytes_per_launch")
+            traffic = json.loads(traffic_file.read_text())
         except ValueError:
-            pass
+            traffic = {}
+        roofline["traffic"] = traffic.get("dram_bytes_per_launch")
+    if roofline["traffic"]:
+        # DRAM-side fraction: the bytes the dominant kernel really moved per
+        # launch (ncu) over the same device time
+        dram_gbs = roofline["traffic"] / (ms_per_step / 1e3) / 1e9
+        roofline["dram"] = {"achieved": dram_gbs, "frac": dram_gbs / roofline["peak"]}
+    if impl == "gb300":
+        # the allocator's own roofline: L2 atomics per second against the
+        # probe's peak, atomics per unit from an ncu count of the same kernel
+        roofline["l2_atomic"] = l2_atomic_roofline(torch, stream, traffic.get("l2_atomics_per_unit"),
+                                                   units / (ms_per_step / 1e3))
 
     result = {
         "metric": {"batches": "malloc+free ops/s (one op = one malloc or one free request)",
@@ -915,6 +961,15 @@ def run(args) -> dict | None:
         result["spill"] = {"host_served": int(st[4]), "host_fraction": int(st[4]) / max(units * args.steps, 1)}
     if ha is not None:
         close_allocator(impl, ha)
+    if impl == "gb300" and a is not None and args.workload in ("mixed", "mixed-slices", "calloc"):
+        # untimed end-state check of the whole run (timed and e2e steps): with
+        # every allocation freed and the pinned blocks flushed, every tree and
+        # table must equal its state after creation
+        a.flush_pinned(s_ptr)
+        torch.cuda.synchronize()
+        rep = a.check_restored()
+        result["checks"] = {"restored": rep["restored"],
+                            "differences": {k: v for k, v in rep.items() if k != "restored" and v}}
     if impl == "gb300" and a is not None:
         st_all = a.stats()
         result["allocator_counters"] = st_all["counters"]

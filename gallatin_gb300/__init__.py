@@ -158,6 +158,27 @@ class _Stats(ctypes.Structure):
     ]
 
 
+class _RestoreReport(ctypes.Structure):
+    _fields_ = [
+        ("segment_tree_words", c_uint64),
+        ("sub_tree_words", c_uint64),
+        ("adopt_tree_words", c_uint64),
+        ("tagged_segments", c_uint64),
+        ("open_segments", c_uint64),
+        ("blocks_out", c_uint64),
+        ("live_blocks", c_uint64),
+        ("taken_slices", c_uint64),
+        ("pinned_slots", c_uint64),
+        ("corrupt", c_uint64),
+        ("bad_frees", c_uint64),
+        ("locks", c_uint32),
+        ("restored", c_uint32),
+    ]
+
+
+SIZE_INFO_DTYPE = np.dtype([("tier", "<u4"), ("tree", "<u4"), ("count", "<u8"), ("allocated", "<u8")])
+TIERS = ("slice", "block", "segment")
+
 VEB_OP_DTYPE = np.dtype([("code", "<u4"), ("tid", "<u4"), ("arg", "<u8"), ("arg2", "<u8")])
 
 _LIB = None
@@ -195,6 +216,11 @@ def load(path: str | Path | None = None):
         "gal_malloc_batch": (i32, [vp, vp, u64, vp, vp]),
         "gal_free_batch": (i32, [vp, vp, u64, vp]),
         "gal_flush_pinned": (i32, [vp, vp]),
+        "gal_size_classes": (i32, [vp, vp, u64, vp, vp]),
+        "gal_check_restored": (i32, [vp, POINTER(_RestoreReport)]),
+        "gal_set_wait_limit": (i32, [vp, u32]),
+        "gal_set_locks": (i32, [vp, u32]),
+        "gal_probe_l2_atomics": (i32, [vp, u64, u32, u32, u32, vp, POINTER(u64), vp]),
         "gal_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
@@ -234,6 +260,20 @@ def _check(rc: int) -> None:
     if rc != 0:
         msg = load().gal_last_error().decode(errors="replace")
         raise GalError(f"gallatin_gb300 call failed ({rc}): {msg}")
+
+
+def probe_l2_atomics(d_words: int, nbytes: int, iters: int, mode: int = 0, ctas_per_sm: int = 8,
+                     d_sink: int = 0, stream: int = 0) -> int:
+    """Launch the L2 atomic throughput probe (gal_probe_l2_atomics) over a
+    device buffer of nbytes (its 128-byte lines, rounded down to a power of
+    two, plus one u64 of it used as the sink); returns the atomics issued."""
+    lines = 1 << ((nbytes // 128).bit_length() - 1)
+    if d_sink == 0:
+        lines //= 2  # keep the sink outside the probed lines
+        d_sink = d_words + lines * 128
+    ops = c_uint64(0)
+    _check(load().gal_probe_l2_atomics(d_words, lines, iters, mode, ctas_per_sm, d_sink, ctypes.byref(ops), stream))
+    return ops.value
 
 
 def _ceil_log2(v: int) -> int:
@@ -559,6 +599,32 @@ class Gallatin:
             "counters": dict(zip(COUNTERS, list(s.counters)[: len(COUNTERS)])),
             "tree_pins": list(s.counters)[TREE_PIN_COUNTER : TREE_PIN_COUNTER + nt],
         }
+
+    def size_classes(self, d_sizes: int, n: int, d_out: int, stream: int = 0) -> None:
+        """Device size classing of n request sizes into n SIZE_INFO_DTYPE
+        records (gal_size_classes): tier, tree, slices or segments, and the
+        allocated bytes (reference get_allocated_size)."""
+        _check(load().gal_size_classes(self.handle, d_sizes, n, d_out, stream))
+
+    def check_restored(self) -> dict:
+        """Differences between the current state and the state after
+        creation (gal_check_restored); "restored" is True when there are none.
+        Call after every allocation is freed and flush_pinned has run."""
+        r = _RestoreReport()
+        _check(load().gal_check_restored(self.handle, ctypes.byref(r)))
+        out = {name: int(getattr(r, name)) for name, _ in _RestoreReport._fields_}
+        out["restored"] = bool(out["restored"])
+        return out
+
+    def set_wait_limit(self, lock_spins: int) -> None:
+        """Tries of the segment-tier lock before a segment-tier malloc returns
+        NULL and counts a timeout (gal_set_wait_limit)."""
+        _check(load().gal_set_wait_limit(self.handle, lock_spins))
+
+    def set_locks(self, locks: int) -> None:
+        """Overwrite the lock word while no kernel runs (gal_set_locks): a
+        bit set here is held by nobody, so waits on it run to their bound."""
+        _check(load().gal_set_locks(self.handle, locks))
 
     def print_info(self) -> None:
         _check(load().gal_print_info(self.handle))

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -163,6 +164,7 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
   s.num_sms = (uint32_t)prop.multiProcessorCount;
   s.seed = seed;
   s.flags = flags;
+  s.lock_spins = GAL_DEFAULT_LOCK_SPINS;
   // Pinned blocks per slot class: one per SM for small trees; for large
   // trees as many as a quarter of the arena split evenly over the trees
   // affords (a block of tree t is 4096 slices of min << t bytes). A run
@@ -455,5 +457,99 @@ extern "C" int gal_print_info(gal_allocator *h) {
          (unsigned long long)st.counters[GAL_CTR_OOM_SEGMENT], (unsigned long long)st.counters[GAL_CTR_TIMEOUT],
          (unsigned long long)st.counters[GAL_CTR_BAD_FREE], (unsigned long long)st.counters[GAL_CTR_CORRUPT]);
   fflush(stdout);
+  return GAL_OK;
+}
+
+extern "C" int gal_set_wait_limit(gal_allocator *h, uint32_t lock_spins) {
+  if (h == nullptr) return fail_invalid("handle is NULL");
+  GAL_CUDA_TRY(cudaDeviceSynchronize(), "wait limit sync");
+  h->hs.lock_spins = lock_spins;
+  GAL_CUDA_TRY(cudaMemcpy((char *)h->d_state + offsetof(gal_state_t, lock_spins), &lock_spins, sizeof(lock_spins),
+                          cudaMemcpyHostToDevice),
+               "wait limit copy");
+  return GAL_OK;
+}
+
+extern "C" int gal_set_locks(gal_allocator *h, uint32_t locks) {
+  if (h == nullptr) return fail_invalid("handle is NULL");
+  GAL_CUDA_TRY(cudaDeviceSynchronize(), "set locks sync");
+  GAL_CUDA_TRY(cudaMemcpy(h->hs.locks, &locks, sizeof(locks), cudaMemcpyHostToDevice), "set locks copy");
+  return GAL_OK;
+}
+
+namespace {
+
+template <class T>
+int copy_down(std::vector<T> &dst, const void *src, uint64_t count, const char *what) {
+  dst.resize(count);
+  if (count == 0) return GAL_OK;
+  GAL_CUDA_TRY(cudaMemcpy(dst.data(), src, count * sizeof(T), cudaMemcpyDeviceToHost), what);
+  return GAL_OK;
+}
+
+// Words of a vEB tree that differ from a full tree (full) or are non-zero.
+int veb_diff(const gal_veb_t &t, bool full, uint64_t *diff) {
+  std::vector<uint64_t> words;
+  for (int layer = 0; layer < t.num_layers; ++layer) {
+    int rc = copy_down(words, t.bits[layer], t.layer_words[layer], "check copy vEB layer");
+    if (rc != GAL_OK) return rc;
+    const uint64_t u = t.layer_universe[layer];
+    for (uint64_t w = 0; w < words.size(); ++w) {
+      uint64_t want = 0;
+      if (full) {
+        const uint64_t left = u - w * 64;
+        want = left >= 64 ? ~0ull : ((1ull << left) - 1);
+      }
+      *diff += words[w] != want;
+    }
+  }
+  return GAL_OK;
+}
+
+}  // namespace
+
+extern "C" int gal_check_restored(gal_allocator *h, gal_restore_report_t *out) {
+  if (h == nullptr || out == nullptr) return fail_invalid("NULL argument");
+  memset(out, 0, sizeof(*out));
+  const gal_state_t &s = h->hs;
+  GAL_CUDA_TRY(cudaDeviceSynchronize(), "check sync");
+  int rc = veb_diff(s.segment_tree, true, &out->segment_tree_words);
+  for (int t = 0; rc == GAL_OK && t < s.num_trees; ++t) rc = veb_diff(s.sub_trees[t], false, &out->sub_tree_words);
+  for (uint32_t k = 0; rc == GAL_OK && k < s.num_classes; ++k) {
+    rc = veb_diff(s.adopt_trees[k], false, &out->adopt_tree_words);
+    if (rc == GAL_OK) rc = veb_diff(s.roomy_trees[k], false, &out->adopt_tree_words);
+  }
+  if (rc != GAL_OK) return rc;
+  std::vector<uint16_t> ids;
+  if ((rc = copy_down(ids, s.chunk_ids, s.num_segments, "check copy chunk_ids")) != GAL_OK) return rc;
+  for (uint16_t id : ids) out->tagged_segments += id != GAL_FREE_SEGMENT;
+  std::vector<int32_t> avail;
+  if ((rc = copy_down(avail, s.seg_avail, s.num_segments, "check copy seg_avail")) != GAL_OK) return rc;
+  for (int32_t a : avail) out->open_segments += a != GAL_SEG_GATE;
+  const uint64_t nblocks = s.num_segments * s.blocks_per_segment;
+  std::vector<uint64_t> words;
+  if ((rc = copy_down(words, s.block_meta, nblocks, "check copy block_meta")) != GAL_OK) return rc;
+  for (uint64_t m : words) {
+    out->blocks_out += ((m >> GAL_META_STATE_SHIFT) & 3u) != GAL_STATE_FREE;
+    out->live_blocks += (m & GAL_META_LIVE_MASK) != 0;
+  }
+  // the slice bitmaps, 64 words per block, in pieces of 1 Mi words
+  const uint64_t total = nblocks * GAL_BLOCK_WORDS;
+  for (uint64_t at = 0; at < total; at += 1ull << 20) {
+    const uint64_t n = total - at < (1ull << 20) ? total - at : (1ull << 20);
+    if ((rc = copy_down(words, s.block_bits + at, n, "check copy block_bits")) != GAL_OK) return rc;
+    for (uint64_t w : words) out->taken_slices += (uint64_t)__builtin_popcountll(~w);
+  }
+  if ((rc = copy_down(words, s.slots, s.total_slots, "check copy slots")) != GAL_OK) return rc;
+  for (uint64_t v : words) out->pinned_slots += v != (uint64_t)GAL_EMPTY_BLOCK;
+  std::vector<unsigned long long> ctr;
+  if ((rc = copy_down(ctr, s.counters, GAL_NUM_COUNTERS, "check copy counters")) != GAL_OK) return rc;
+  out->corrupt = ctr[GAL_CTR_CORRUPT];
+  out->bad_frees = ctr[GAL_CTR_BAD_FREE];
+  GAL_CUDA_TRY(cudaMemcpy(&out->locks, s.locks, sizeof(uint32_t), cudaMemcpyDeviceToHost), "check copy locks");
+  out->restored = out->segment_tree_words == 0 && out->sub_tree_words == 0 && out->adopt_tree_words == 0 &&
+                  out->tagged_segments == 0 && out->open_segments == 0 && out->blocks_out == 0 &&
+                  out->live_blocks == 0 && out->taken_slices == 0 && out->pinned_slots == 0 && out->corrupt == 0 &&
+                  out->bad_frees == 0 && out->locks == 0;
   return GAL_OK;
 }

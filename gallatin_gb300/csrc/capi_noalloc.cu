@@ -11,8 +11,6 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "capi_internal.h"
 
 namespace {
@@ -25,23 +23,15 @@ constexpr uint64_t kScratchBytes = GAL_NOALLOC_TRACE_MAX_BYTES + 256;
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void *g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (that first lookup is the only set-up this entry point does).
+// Device address of the scratch array in the current device's context. It
+// is looked up on every call, so a context made after cudaDeviceReset gets
+// its own array's address rather than a stale one. Under CUDA's default lazy
+// module loading, the first lookup on a device also loads the module that
+// holds the array, which is when the driver commits its memory.
 int scratch_for_current_device(uint8_t **out) {
-  int dev = 0;
-  GAL_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) return galcapi::fail_invalid("device ordinal out of range");
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_ptr[dev] == nullptr) {
-    void *ptr = nullptr;
-    GAL_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)");
-    g_scratch_ptr[dev] = ptr;
-  }
-  *out = (uint8_t *)g_scratch_ptr[dev];
+  void *ptr = nullptr;
+  GAL_CUDA_TRY(cudaGetSymbolAddress(&ptr, g_noalloc_scratch), "cudaGetSymbolAddress(noalloc scratch)");
+  *out = (uint8_t *)ptr;
   return GAL_OK;
 }
 

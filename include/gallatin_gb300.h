@@ -133,12 +133,76 @@ int gal_dump(gal_allocator *h, int which, int tree, int layer, void *host_dst, u
  * GAL_DUMP_ROOMY_TREE (tree selects the slot class) */
 int gal_veb_layer_count(gal_allocator *h, int which, int tree);
 
+/* End-state check: after every allocation is freed and gal_flush_pinned
+ * has run (no kernel running), compare every tree and table with the state
+ * gal_create left and count the differences. The reference has no such
+ * check; its tests count live slices per block (tests/src/
+ * gallatin_host_test.cu:87-95, check_overlaps_kernel). restored is 1 when
+ * every count is zero. */
+typedef struct gal_restore_report_t {
+  uint64_t segment_tree_words; /* segment tree words that differ from a full tree */
+  uint64_t sub_tree_words;     /* non-zero words of the per-size sub trees */
+  uint64_t adopt_tree_words;   /* non-zero words of the adoptable and roomy trees */
+  uint64_t tagged_segments;    /* memory-table entries not marked free */
+  uint64_t open_segments;      /* segments whose free-block count is not at the gate */
+  uint64_t blocks_out;         /* blocks not in their segment's pool */
+  uint64_t live_blocks;        /* blocks whose live count is not zero */
+  uint64_t taken_slices;       /* slices whose bitmap bit is not back to free */
+  uint64_t pinned_slots;       /* pinned-block slots not empty */
+  uint64_t corrupt;            /* GAL_CTR_CORRUPT */
+  uint64_t bad_frees;          /* GAL_CTR_BAD_FREE */
+  uint32_t locks;              /* the lock word */
+  uint32_t restored;
+} gal_restore_report_t;
+int gal_check_restored(gal_allocator *h, gal_restore_report_t *out);
+
+/* Bound on the segment-tier lock wait: a segment-tier malloc (a request
+ * larger than one segment) that cannot take the lock in lock_spins tries
+ * (with a backoff growing to ~1 us per try) returns NULL and counts
+ * GAL_CTR_TIMEOUT. Default GAL_DEFAULT_LOCK_SPINS, about a second; no kernel
+ * may run during the call. The reference waits on this lock without bound
+ * (gallatin.cuh:796). */
+int gal_set_wait_limit(gal_allocator *h, uint32_t lock_spins);
+
+/* Overwrite the lock word (bit t: tree t's segment-attach lock, bit 31: the
+ * segment-tier lock) while no kernel runs. A bit set here is held by no
+ * thread, so every wait on it runs to its bound: this is how the tests show
+ * that the waits end, without a GPU fault or hang. Clear it again (0)
+ * before normal use. No counterpart in the reference. */
+int gal_set_locks(gal_allocator *h, uint32_t locks);
+
 /* --- batch entry points (device buffers, one thread per request) ---
  * These are the host-callable form of Gallatin::malloc / free
  * (gallatin.cuh:1186,1378), as the reference tests drive them from
  * kernels (tests/src/gallatin_test.cu:58-112). */
 int gal_malloc_batch(gal_allocator *h, const uint64_t *d_sizes, uint64_t n, uint64_t *d_ptrs, void *stream);
 int gal_free_batch(gal_allocator *h, const uint64_t *d_ptrs, uint64_t n, void *stream);
+
+/* Size classing as the device computes it, one entry per request size:
+ * tier 0 = slices (tree = size class, count = slices per request), 1 = a
+ * whole block (tree = block tree, count 1), 2 = contiguous segments
+ * (count = segments); allocated = the bytes the request occupies. Replaces
+ * the reference's device get_tree_id_from_size / malloc dispatch /
+ * get_allocated_size (gallatin.cuh:1141-1183, 1196-1260), which have no host
+ * entry point there. d_sizes and d_out are device buffers of n entries. */
+typedef struct gal_size_info_t {
+  uint32_t tier;
+  uint32_t tree;
+  uint64_t count;
+  uint64_t allocated;
+} gal_size_info_t;
+int gal_size_classes(gal_allocator *h, const uint64_t *d_sizes, uint64_t n, gal_size_info_t *d_out, void *stream);
+
+/* L2 atomic throughput probe (the denominator of the allocator's atomic
+ * roofline; no counterpart in the reference). ctas_per_sm CTAs of 256 threads
+ * per SM; lane 0 of each warp issues `iters` rounds of 8 independent 64-bit
+ * atomic adds, each to its own 128-byte line of d_words (lines * 128 bytes,
+ * lines a power of two, at least the number of warps): mode 0 atom (returns
+ * the old value, as the allocator's reservations do), mode 1 red (no return,
+ * as its bitmap returns do). *ops_out = atomics the launch issues; time it on
+ * `stream` with events. d_sink: one device u64 the kernel may write. */
+int gal_probe_l2_atomics(uint64_t *d_words, uint64_t lines, uint32_t iters, uint32_t mode, uint32_t ctas_per_sm,
+                         unsigned long long *d_sink, uint64_t *ops_out, void *stream);
 
 /* Detach every pinned block (no malloc/free may run concurrently). Empty
  * blocks and segments return to their pools, so after all allocations are
@@ -172,11 +236,14 @@ int gal_run_mixed_host(gal_allocator *h, uint64_t n_threads, uint32_t rounds, ui
  * bytes compiled into the library, which every GPU that loads the library
  * holds until the process exits; traces larger than
  * GAL_NOALLOC_TRACE_MAX_BYTES (n_threads * rounds) are rejected with
- * GAL_ERR_INVALID. The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the one array: calls whose GPU work overlaps
- * (other streams, other host threads) race on it. No counterpart in the
- * reference, which allocates its buffers with cudaMalloc. */
+ * GAL_ERR_INVALID. Each call looks up the array's device address
+ * (cudaGetSymbolAddress). Under CUDA's default lazy module loading the first
+ * call on a device also loads the module holding the array, and that is when
+ * the driver takes its memory: make that first call before the device's
+ * memory is divided up and before any stream capture, or set
+ * CUDA_MODULE_LOADING=EAGER. All calls share the one array: calls whose GPU
+ * work overlaps (other streams, other host threads) race on it. No
+ * counterpart in the reference, which allocates its buffers with cudaMalloc. */
 #define GAL_NOALLOC_TRACE_MAX_BYTES (2ull << 20)
 int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64_t seed,
                                uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,

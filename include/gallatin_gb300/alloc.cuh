@@ -35,12 +35,20 @@
 #include "state.h"
 #include "veb.cuh"
 
+// Marks the paths taken once per block or segment change (slot replacement,
+// the block and segment tiers). They are inlined by default: compiled out of
+// line (-DGAL_COLD=__noinline__) they shrink the calling kernels and their
+// build time by about ten times, but the calls cost the mixed workload 14 %
+// and the plain 16 B workload 11 % on a GB300 (the hash table was level).
+#ifndef GAL_COLD
+#define GAL_COLD
+#endif
+
 namespace gal {
 
 constexpr int kSliceAttempts = 4096;      // group attempts per slice request
 constexpr int kClaimSteps = 256;          // fetch-and steps per reservation
 constexpr int kRequestBlockAttempts = 512;
-constexpr int kSegmentLockSpins = 1 << 20;
 constexpr int kSegmentLockBit = 31;
 // a pinned block past this many live slices is replaced ahead of time, so
 // warps rarely find their slot's block full
@@ -357,17 +365,22 @@ __device__ inline void try_retire_block(const gal_state_t *st, uint64_t b) {
 // Give back n slices of block b's live count and act on the transitions.
 // `ordered`: the caller has already fenced (free_slice), so the add itself
 // can be relaxed.
+__device__ inline void after_release(const gal_state_t *st, uint64_t b, uint32_t n, uint64_t old) {
+  const uint32_t live = meta_live(old);
+  if (live == n) {
+    try_retire_block(st, b);
+  } else if (meta_state(old) == GAL_STATE_DETACHED && live > GAL_ROOMY_MARK && live - n <= GAL_ROOMY_MARK) {
+    adopt_sync(st, meta_class(old), b, true);
+  }
+}
+
 __device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n, bool ordered = false) {
   const uint64_t delta = (uint64_t)(-(int64_t)n);
   const uint64_t old =
       ordered ? ptx::atom_add_relaxed(st->block_meta + b, delta) : ptx::atom_add_release(st->block_meta + b, delta);
-  const uint32_t state = meta_state(old);
-  const uint32_t live = meta_live(old);
-  if ((state == GAL_STATE_DETACHED || state == GAL_STATE_WHOLE) && live == n) {
-    try_retire_block(st, b);
-  } else if (state == GAL_STATE_DETACHED && live > GAL_ROOMY_MARK && live - n <= GAL_ROOMY_MARK) {
-    adopt_sync(st, meta_class(old), b, true);
-  }
+  // a PINNED block has nothing to do; DETACHED and WHOLE ones may retire or
+  // become roomy
+  if (meta_state(old) >= GAL_STATE_DETACHED) after_release(st, b, n, old);
 }
 
 // Move a block this thread owns from FREE to `state`, formatted for tree t
@@ -443,7 +456,7 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
 // newly attached one; with ADOPT_ANY, when the arena has neither, a detached
 // block with any room. An adopted block is already PINNED (*adopted = true).
 // GAL_EMPTY_BLOCK when nothing can be had.
-__device__ inline uint32_t request_block(const gal_state_t *st, uint32_t t, uint32_t k, uint32_t c, uint64_t tid,
+__device__ inline GAL_COLD uint32_t request_block(const gal_state_t *st, uint32_t t, uint32_t k, uint32_t c, uint64_t tid,
                                          int adopt_mode, bool *adopted) {
   *adopted = false;
   if (adopt_mode >= ADOPT_ROOMY) {
@@ -506,7 +519,7 @@ __device__ inline void pin_block(const gal_state_t *st, uint64_t b, uint32_t t, 
   count(st, GAL_CTR_TREE_PINS + (int)t);
 }
 
-__device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) {
+__device__ inline void detach_block(const gal_state_t *st, uint64_t b) {
   const uint64_t old = ptx::atom_add_release(
       st->block_meta + b, (uint64_t)(GAL_STATE_DETACHED - GAL_STATE_PINNED) << GAL_META_STATE_SHIFT);
   if (meta_live(old) == 0) {
@@ -521,7 +534,7 @@ __device__ __forceinline__ void detach_block(const gal_state_t *st, uint64_t b) 
 // Replace the block a slot holds (`seen`, without the REPLACING flag) by
 // another pinned one. Only the thread whose CAS sets REPLACING does the work;
 // REPLACE_NOMEM when request_block found nothing (the slot is left as seen).
-__device__ inline int replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t, uint32_t r,
+__device__ inline GAL_COLD int replace_slot(const gal_state_t *st, uint64_t *slot, uint64_t seen, uint32_t t, uint32_t r,
                                    int adopt_mode, uint32_t *out) {
   // the hashed search starts come from the thread id, read here rather than
   // carried through the claim loop
@@ -820,7 +833,7 @@ __device__ inline void free_slice(const gal_state_t *st, uint64_t seg, uint32_t 
 
 // ---- block and segment tiers ---------------------------------------------
 
-__device__ inline void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_t tid) {
+__device__ inline GAL_COLD void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_t tid) {
   bool adopted = false;
   const uint32_t b = request_block(st, bt, 0, 1, tid, ADOPT_NONE, &adopted);
   if (b == GAL_EMPTY_BLOCK) {
@@ -831,19 +844,20 @@ __device__ inline void *malloc_block(const gal_state_t *st, uint32_t bt, uint64_
   return block_address(st, b, bt);
 }
 
-__device__ inline void *malloc_segment(const gal_state_t *st, uint64_t nseg) {
+__device__ inline GAL_COLD void *malloc_segment(const gal_state_t *st, uint64_t nseg) {
   const uint64_t max_n = 0xFFFEull - (uint64_t)st->num_trees - 1;
   if (nseg > st->num_segments || nseg > max_n) {
     count(st, GAL_CTR_OOM_SEGMENT);
     return nullptr;
   }
-  int spins = 0;
+  // the reference spins on this lock without bound (gallatin.cuh:796)
+  uint32_t spins = 0;
   while (!try_lock(st, kSegmentLockBit)) {
-    if (++spins >= kSegmentLockSpins) {
+    if (++spins >= st->lock_spins) {
       count(st, GAL_CTR_TIMEOUT);
       return nullptr;
     }
-    backoff(spins);
+    backoff((int)(spins < 4096 ? spins : 4096));
   }
   const uint64_t first = veb::gather_run(&st->segment_tree, nseg);
   unlock(st, kSegmentLockBit);
@@ -860,7 +874,7 @@ __device__ inline void *malloc_segment(const gal_state_t *st, uint64_t nseg) {
   return st->memory + (first << st->segment_shift);
 }
 
-__device__ inline void free_segment(const gal_state_t *st, uint64_t seg, uint16_t id) {
+__device__ inline GAL_COLD void free_segment(const gal_state_t *st, uint64_t seg, uint16_t id) {
   const uint64_t n = (uint64_t)id - (uint64_t)st->num_trees - 1;
   if (atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)id, (unsigned short)GAL_FREE_SEGMENT) !=
       (unsigned short)id) {
@@ -897,24 +911,33 @@ __device__ inline void zero_ranges(uint32_t active, char *p, uint64_t bytes) {
 
 // Bytes a live allocation at arena offset `off` spans, read from the
 // metadata that free uses (0 for a pointer free would reject): the slice run
-// of its block, a whole block-tier block, or its segments.
+// of its block, a whole block-tier block, or its segments. The span never
+// reaches past the end of the block (slice and block tiers) or of the arena
+// (segment tier) that holds `off`, so even a pointer that was freed twice,
+// whose block words may no longer describe it, cannot make the zeroing
+// write outside the arena.
 __device__ inline uint64_t allocation_span(const gal_state_t *st, uint64_t off) {
   if (off >= st->arena_bytes) return 0;
   const uint64_t seg = off >> st->segment_shift;
   const uint16_t id = st->chunk_ids[seg];
   if (id < (uint16_t)st->num_trees) {
     const uint32_t t = id;
-    const uint64_t b = (seg << block_index_shift(st)) + ((off & (st->segment_bytes - 1)) >> (st->block_shift_min + (int)t));
+    const int block_shift = st->block_shift_min + (int)t;
+    const uint64_t b = (seg << block_index_shift(st)) + ((off & (st->segment_bytes - 1)) >> block_shift);
     // state (WHOLE or not) and run length cannot change while the allocation
     // is live; read past L1 all the same
     const uint64_t m = ptx::ld_relaxed(st->block_meta + b);
     const int slice_shift = st->min_shift + (int)t;
-    if (meta_state(m) == GAL_STATE_WHOLE) return (uint64_t)GAL_BLOCK_SLICES << slice_shift;
-    const uint64_t c = (t == (uint32_t)st->num_trees - 1) ? (1ull << meta_run(m)) : 1ull;
-    return c << slice_shift;
+    const uint64_t room = (1ull << block_shift) - (off & ((1ull << block_shift) - 1));
+    uint64_t span = (uint64_t)GAL_BLOCK_SLICES << slice_shift;
+    if (meta_state(m) != GAL_STATE_WHOLE)
+      span = ((t == (uint32_t)st->num_trees - 1) ? (1ull << meta_run(m)) : 1ull) << slice_shift;
+    return span < room ? span : room;
   }
-  if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees)
-    return ((uint64_t)id - (uint64_t)st->num_trees - 1) << st->segment_shift;
+  if (id != GAL_FREE_SEGMENT && id > (uint16_t)st->num_trees) {
+    const uint64_t span = ((uint64_t)id - (uint64_t)st->num_trees - 1) << st->segment_shift;
+    return span < st->arena_bytes - off ? span : st->arena_bytes - off;
+  }
   return 0;
 }
 

@@ -80,6 +80,9 @@ __device__ __forceinline__ void red_or_release(uint64_t *p, uint64_t v) {
 __device__ __forceinline__ void red_or_relaxed(uint64_t *p, uint64_t v) {
   asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+__device__ __forceinline__ void red_add_relaxed(uint64_t *p, uint64_t v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 __device__ __forceinline__ void red_and_relaxed(uint64_t *p, uint64_t v) {
   asm volatile("red.relaxed.gpu.global.and.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }

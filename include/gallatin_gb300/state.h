@@ -80,6 +80,10 @@
                                   can be handed out again, so malloc returns zeroed memory (reference
                                   running_calloc, gallatin.cuh:1306-1369) */
 
+/* default bound on the segment-tier lock wait: 2^20 tries with a backoff of
+ * up to ~1 us each, about a second */
+#define GAL_DEFAULT_LOCK_SPINS (1u << 20)
+
 /* slot word: low 32 bits block id (GAL_EMPTY_BLOCK when none), bit 32 set
  * while one leader is replacing the block. */
 #define GAL_SLOT_REPLACING (1ull << 32)
@@ -136,6 +140,9 @@ typedef struct gal_state_t {
   uint32_t num_sms;
   uint32_t total_slots;
   uint32_t flags;                  /* GAL_FLAG_* */
+  uint32_t lock_spins;             /* tries of the segment-tier lock before a
+                                      segment-tier malloc gives up (NULL and
+                                      GAL_CTR_TIMEOUT); GAL_DEFAULT_LOCK_SPINS */
   uint32_t slot_count[GAL_MAX_TREES];
   uint32_t slot_offset[GAL_MAX_TREES];
   uint64_t seed;

@@ -110,10 +110,16 @@ def make_arena(nbytes, seed, host):
     return make(nbytes, seed, print_info=False)
 
 
+# the capacity and out-of-memory results depend on how concurrent claims
+# race, so each such test runs several times per session
+REPEATS = 8
+
+
+@pytest.mark.parametrize("rep", range(REPEATS))
 @pytest.mark.parametrize("host", [False, True], ids=["device-arena", "host-arena"])
-def test_slice_tier_fills_to_capacity_then_returns_null(cuda, host):
+def test_slice_tier_fills_to_capacity_then_returns_null(cuda, host, rep):
     # 4 segments of 16 MiB; a 4 KiB block is a whole segment: 4 * 4096 slices
-    with make_arena(64 << 20, 3, host) as a:
+    with make_arena(64 << 20, 3 + rep, host) as a:
         cap = 4 * 4096
         sizes = np.full(cap + 100, 4096, dtype=np.uint64)
         ptrs = malloc_batch(cuda, a, sizes)
@@ -123,9 +129,10 @@ def test_slice_tier_fills_to_capacity_then_returns_null(cuda, host):
         release_all(cuda, a, ptrs)
 
 
+@pytest.mark.parametrize("rep", range(REPEATS // 2))
 @pytest.mark.parametrize("host", [False, True], ids=["device-arena", "host-arena"])
-def test_block_and_segment_tiers_exact_capacity(cuda, host):
-    with make_arena(64 << 20, 4, host) as a:
+def test_block_and_segment_tiers_exact_capacity(cuda, host, rep):
+    with make_arena(64 << 20, 4 + rep, host) as a:
         ptrs = malloc_batch(cuda, a, np.full(5, 16 << 20, dtype=np.uint64))  # whole-segment blocks
         assert int((ptrs != 0).sum()) == 4
         free_batch(cuda, a, ptrs)
@@ -203,3 +210,48 @@ def test_allocated_size_spans_are_disjoint_per_class(cuda):
     with gal.Gallatin.generate_on_device(256 << 20, 2, print_info=False) as a:
         for size in (16, 4096, 8192, 40000):
             assert class_bytes(a, size) >= size
+
+
+def test_restore_report_agrees_with_the_host_check(cuda):
+    """gal_check_restored sees what check_restored sees: a live allocation
+    (negative control), then nothing once it is freed and the slots flushed."""
+    with gal.Gallatin.generate_on_device(256 << 20, 21, print_info=False) as a:
+        sizes = np.array([16, 4096, 8192, 100_000, 40 << 20], dtype=np.uint64)
+        ptrs = malloc_batch(cuda, a, sizes)
+        assert (ptrs != 0).all()
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        rep = a.check_restored()
+        assert not rep["restored"]
+        assert rep["tagged_segments"] >= 4 and rep["live_blocks"] >= 3 and rep["taken_slices"] >= 3, rep
+        with pytest.raises(AssertionError):
+            check_restored(a)
+        release_all(cuda, a, ptrs)
+        rep = a.check_restored()
+        assert rep["restored"], rep
+
+
+def test_mixed_full_configuration_restores_the_initial_state(cuda):
+    """The mixed-size configuration at full size: an 8 GiB arena, 4,194,304
+    threads x 8 rounds of malloc / fill / verify / free over 16..4096 B, plus
+    256 segment-tier requests of 16-256 MiB. No NULL, no verify failure, and
+    after the pinned blocks are flushed every tree and table is back in its
+    initial state."""
+    from gallatin_gb300.workload import mixed_class_trace
+
+    n, rounds = 4_194_304, 8
+    trace = mixed_class_trace(n, rounds, 42)
+    with gal.Gallatin.generate_on_device(8 << 30, 42, print_info=False) as a:
+        d_trace = cuda.from_numpy(trace.reshape(-1)).cuda()
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        a.run_mixed(n, rounds, 42, stats.data_ptr(), seg_every=64, seg_lo=16 << 20, seg_hi=256 << 20,
+                    d_classes=d_trace.data_ptr(), block_dim=256)
+        cuda.cuda.synchronize()
+        st = stats.cpu().numpy()
+        assert st[0] == 0 and st[1] == 0, f"misses / verify failures: {st}"
+        assert st[2] + st[3] == n // 256 // 64
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        rep = a.check_restored()
+        assert rep["restored"], rep
+        check_restored(a)

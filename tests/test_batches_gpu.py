@@ -131,10 +131,11 @@ def test_long_lived_random_frees_fit_half_full_arena(cuda, persistent, binned):
         check_restored(a)
 
 
-def test_binned_path_serves_each_request_like_the_plain_path(cuda):
+@pytest.mark.parametrize("rep", range(3))
+def test_binned_path_serves_each_request_like_the_plain_path(cuda, rep):
     """Binning only reorders a batch: every malloc gets a block of its own
     size class and the live set after each form is the same set of slots."""
-    reqs, offsets, slots, info = small_trace(13)
+    reqs, offsets, slots, info = small_trace(13 + rep)
     tables = []
     for persistent, binned in [(False, False), (True, True)]:
         with gal.Gallatin.generate_on_device(1 << 30, 8, print_info=False) as a:
@@ -156,15 +157,16 @@ def test_binned_path_serves_each_request_like_the_plain_path(cuda):
     assert np.array_equal(tables[0], tables[1])
 
 
+@pytest.mark.parametrize("rep", range(3))
 @pytest.mark.parametrize("arena_mib,calloc,binned", [(64, False, False), (128, False, True), (64, True, True)],
                          ids=["64MiB-plain", "128MiB-binned", "64MiB-calloc-binned"])
-def test_batches_in_an_arena_too_small_for_the_stream(cuda, arena_mib, calloc, binned):
+def test_batches_in_an_arena_too_small_for_the_stream(cuda, arena_mib, calloc, binned, rep):
     # the stream's live set peaks near 90 MB in class bytes, over nine slice
     # trees and the block tier: a 4- or 8-segment arena runs out. Mallocs
     # return NULL (the strike path), what was served must still be a valid
     # live set, frees of NULL slots are no-ops, and the drain restores the state
     reqs, offsets, slots, info = small_trace(11)
-    with gal.Gallatin.generate_on_device(arena_mib << 20, 6, print_info=False, running_calloc=calloc) as a:
+    with gal.Gallatin.generate_on_device(arena_mib << 20, 6 + rep, print_info=False, running_calloc=calloc) as a:
         d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
         d_offs = cuda.from_numpy(offsets.view(np.int64)).cuda()
         d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")

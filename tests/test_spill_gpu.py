@@ -48,14 +48,15 @@ def run_fill_drain(cuda, dev, host, classes, check_filled=None):
     return ptrs, fill_stats, d_stats.cpu().numpy(), d_table.cpu().numpy()
 
 
-def test_fused_spills_to_the_host_arena_and_restores_both(cuda):
+@pytest.mark.parametrize("rep", range(4))
+def test_fused_spills_to_the_host_arena_and_restores_both(cuda, rep):
     # 4 device segments cannot hold 131,072 mixed allocations (~113 MiB):
     # the rest must land in the host arena, and every pointer must verify
-    dev = gal.Gallatin.generate_on_device(64 << 20, 3, print_info=False)
-    host = gal.Gallatin.generate_on_device_host(512 << 20, 4, print_info=False)
+    dev = gal.Gallatin.generate_on_device(64 << 20, 3 + rep, print_info=False)
+    host = gal.Gallatin.generate_on_device_host(512 << 20, 4 + rep, print_info=False)
     try:
         assert host.host_arena and not dev.host_arena
-        classes = fill_sizes(1 << 17, 11)
+        classes = fill_sizes(1 << 17, 11 + rep)
         sizes = (np.uint64(16) << classes.astype(np.uint64))
         where = {}
 
@@ -115,6 +116,13 @@ def test_host_arena_bytes_are_visible_to_the_cpu(cuda):
         cuda.cuda.synchronize()
         ptrs = d_table.cpu().numpy().view(np.uint64)
         assert (ptrs != 0).all()
+        # the CPU dereferences these addresses: every allocation must lie
+        # inside the host arena first, so a bad pointer fails the test
+        # instead of faulting the process
+        sizes = np.uint64(16) << classes.astype(np.uint64)
+        lo, hi = host.arena_base, host.arena_base + host.arena_bytes
+        inside = (ptrs >= np.uint64(lo)) & (ptrs + sizes <= np.uint64(hi))
+        assert inside.all(), f"{int((~inside).sum())} allocations outside the host arena"
         for i in range(0, n, 97):
             size = 16 << int(classes[i])
             first = ctypes.c_uint64.from_address(int(ptrs[i])).value
@@ -216,8 +224,9 @@ def test_calloc_batches_stream(cuda):
         a.free_on_device()
 
 
+@pytest.mark.parametrize("rep", range(4))
 @pytest.mark.parametrize("calloc", [False, True], ids=["plain", "calloc"])
-def test_mixed_rounds_in_a_full_arena_never_share_a_slice(cuda, calloc):
+def test_mixed_rounds_in_a_full_arena_never_share_a_slice(cuda, calloc, rep):
     # 262,144 threads x 4 rounds of malloc / fill / verify / free against 4
     # segments: most rounds find the arena full. Any slice handed to two
     # owners at once shows up as a verify failure (each fills it with its own
@@ -225,7 +234,7 @@ def test_mixed_rounds_in_a_full_arena_never_share_a_slice(cuda, calloc):
     a = gal.Gallatin.generate_on_device(64 << 20, 31, print_info=False, running_calloc=calloc)
     try:
         d_stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
-        a.run_mixed(1 << 18, 4, 9, d_stats.data_ptr())
+        a.run_mixed(1 << 18, 4, 9 + rep, d_stats.data_ptr())
         cuda.cuda.synchronize()
         st = d_stats.cpu().numpy()
         assert st[STAT_MISS] > 0 and st[STAT_BAD] == 0, st
