@@ -73,6 +73,8 @@ OPS = {
     "gather_multiple": 11,
     "return_multiple": 12,
     "report_fill": 13,
+    "find_at_or_after": 14,
+    "claim_first": 15,
 }
 
 DUMP = {
@@ -176,6 +178,37 @@ class _RestoreReport(ctypes.Structure):
     ]
 
 
+class _BenchArgs(ctypes.Structure):
+    _fields_ = [
+        ("workload", c_uint32),
+        ("block_dim", c_uint32),
+        ("n_threads", c_uint64),
+        ("size", c_uint64),
+        ("rounds", c_uint32),
+        ("seg_every", c_uint32),
+        ("seed", c_uint64),
+        ("seg_lo", c_uint64),
+        ("seg_hi", c_uint64),
+        ("d_classes", c_void_p),
+        ("h_classes", c_void_p),
+        ("warmup", c_uint32),
+        ("steps", c_uint32),
+        ("flush_bytes", c_uint64),
+        ("stream", c_void_p),
+    ]
+
+
+class _BenchResult(ctypes.Structure):
+    _fields_ = [
+        ("step_ms", ctypes.POINTER(ctypes.c_float)),
+        ("e2e_step_ms", ctypes.POINTER(ctypes.c_float)),
+        ("stats", c_uint64 * 8),
+        ("e2e_stats", c_uint64 * 8),
+    ]
+
+
+BENCH_WORKLOADS = {"pairs": 0, "mixed": 1}
+
 SIZE_INFO_DTYPE = np.dtype([("tier", "<u4"), ("tree", "<u4"), ("count", "<u8"), ("allocated", "<u8")])
 TIERS = ("slice", "block", "segment")
 
@@ -221,6 +254,7 @@ def load(path: str | Path | None = None):
         "gal_set_wait_limit": (i32, [vp, u32]),
         "gal_set_locks": (i32, [vp, u32]),
         "gal_probe_l2_atomics": (i32, [vp, u64, u32, u32, u32, vp, POINTER(u64), vp]),
+        "gal_bench": (i32, [vp, POINTER(_BenchArgs), POINTER(_BenchResult)]),
         "gal_run_pairs": (i32, [vp, u64, u64, u32, vp, vp]),
         "gal_run_mixed": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
         "gal_run_mixed_host": (i32, [vp, u64, u32, u64, u32, u64, u64, vp, u32, vp, vp]),
@@ -598,6 +632,26 @@ class Gallatin:
             "segments_in_allocations": s.segments_in_allocations,
             "counters": dict(zip(COUNTERS, list(s.counters)[: len(COUNTERS)])),
             "tree_pins": list(s.counters)[TREE_PIN_COUNTER : TREE_PIN_COUNTER + nt],
+        }
+
+    def bench(self, workload: str, n_threads: int, *, steps: int, warmup: int, flush_bytes: int,
+              block_dim: int = 256, size: int = 16, rounds: int = 1, seed: int = 42, seg_every: int = 0,
+              seg_lo: int = 16 << 20, seg_hi: int = 256 << 20, d_classes: int = 0, h_classes: int = 0,
+              stream: int = 0) -> dict:
+        """The native benchmark driver (gal_bench): warm-up, L2 flush before
+        every timed step, CUDA-event device times, and with h_classes (a pinned
+        host trace) the same steps end to end with host-clock times."""
+        args = _BenchArgs(BENCH_WORKLOADS[workload], block_dim, n_threads, size, rounds, seg_every, seed, seg_lo,
+                          seg_hi, d_classes or None, h_classes or None, warmup, steps, flush_bytes, stream or None)
+        step_ms = (ctypes.c_float * steps)()
+        e2e_ms = (ctypes.c_float * steps)() if h_classes else None
+        res = _BenchResult(step_ms, e2e_ms, (c_uint64 * 8)(), (c_uint64 * 8)())
+        _check(load().gal_bench(self.handle, ctypes.byref(args), ctypes.byref(res)))
+        return {
+            "step_ms": list(step_ms),
+            "e2e_step_ms": list(e2e_ms) if e2e_ms is not None else None,
+            "stats": np.array(list(res.stats), dtype=np.uint64),
+            "e2e_stats": np.array(list(res.e2e_stats), dtype=np.uint64),
         }
 
     def size_classes(self, d_sizes: int, n: int, d_out: int, stream: int = 0) -> None:

@@ -17,7 +17,8 @@ REPO_DIR = PKG_DIR.parent
 CSRC = PKG_DIR / "csrc"
 BUILD_DIR = PKG_DIR / "_build"
 LIB_NAME = "libgallatin_gb300.so"
-SOURCES = ["capi_host.cu", "capi_run.cu", "capi_veb.cu", "capi_noalloc.cu", "capi_batch.cu", "capi_serve.cu",
+SOURCES = ["capi_host.cu", "capi_run.cu", "capi_veb.cu", "capi_noalloc.cu", "capi_bench.cu", "capi_batch.cu",
+           "capi_serve.cu",
            "capi_ds.cu", "capi_spill.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -71,12 +71,16 @@ int build_veb(gal_veb_t *t, uint64_t universe, uint64_t seed, bool full, std::ve
     const uint64_t words = (u - 1) / 64 + 1;
     t->layer_universe[layer] = u;
     t->layer_words[layer] = words;
+    // an even number of words, the last one zero when words is odd, so the
+    // allocator's searches can read any aligned pair of words in one 128-bit
+    // load (no bit is ever set past the layer's universe)
+    const uint64_t padded = (words + 1) & ~1ull;
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, words * sizeof(uint64_t));
+    cudaError_t e = cudaMalloc(&p, padded * sizeof(uint64_t));
     if (e != cudaSuccess) return fail_cuda(e, "cudaMalloc vEB layer");
     allocs.push_back(p);
     t->bits[layer] = (uint64_t *)p;
-    std::vector<uint64_t> host(words, 0);
+    std::vector<uint64_t> host(padded, 0);
     if (full) {
       for (uint64_t w = 0; w < words; ++w) {
         const uint64_t lo = w * 64;
@@ -84,7 +88,7 @@ int build_veb(gal_veb_t *t, uint64_t universe, uint64_t seed, bool full, std::ve
         host[w] = left >= 64 ? ~0ull : ((1ull << left) - 1);
       }
     }
-    e = cudaMemcpy(p, host.data(), words * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(p, host.data(), padded * sizeof(uint64_t), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail_cuda(e, "cudaMemcpy vEB layer");
     u = (u - 1) / 64 + 1;
   }
@@ -156,7 +160,9 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
   s.num_trees = num_trees;
   s.block_shift_min = min_shift + 12;
   s.blocks_per_segment = (uint32_t)(segment_bytes >> s.block_shift_min);
-  s.seg_block_words = (s.blocks_per_segment + 63) / 64;
+  // even, so a segment's free-block words start 16-byte aligned and can be
+  // read in pairs (a word past blocks_per_segment stays zero)
+  s.seg_block_words = ((s.blocks_per_segment + 63) / 64 + 1) & ~1u;
   // the largest tree serves runs of 1, 2, 4 ... slices up to half the
   // smallest block (min_size << 11 bytes), one slot class per run length
   const int max_run = 12 - num_trees > 0 ? 12 - num_trees : 0;

@@ -23,6 +23,8 @@ __device__ uint64_t run_one(const gal_veb_t *t, const gal_veb_op &op) {
     case GAL_VEB_OP_MALLOC: return v::malloc_random(t, v::thread_tid());
     case GAL_VEB_OP_GATHER: return v::gather_run(t, op.arg);
     case GAL_VEB_OP_RETURN: v::return_run(t, op.arg, op.arg2); return 0;
+    case GAL_VEB_OP_FIND_AT_OR_AFTER: return v::find_at_or_after(t, op.arg);
+    case GAL_VEB_OP_CLAIM_FIRST: return v::claim_first(t);
     case GAL_VEB_OP_REPORT_FILL: {
       const int leaf = t->num_layers - 1;
       uint64_t fill = 0;

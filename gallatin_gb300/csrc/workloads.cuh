@@ -39,10 +39,6 @@ namespace galwork {
 
 enum { STAT_MISS = 0, STAT_BAD = 1, STAT_SEG_OK = 2, STAT_SEG_MISS = 3, STAT_WORDS = 8 };
 
-// 512-byte steps of the mixed workload's fill whose stores are issued
-// before their read-back loads are consumed
-constexpr uint32_t kFillSteps = 4;
-
 __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   x += 0x9E3779B97F4A7C15ull;
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -60,7 +56,7 @@ __host__ __device__ __forceinline__ uint64_t xorshift64(uint64_t &s) {
 // 16-byte load that the compiler cannot fold into the preceding stores.
 __device__ __forceinline__ ulonglong2 load_cg(const ulonglong2 *p) {
   ulonglong2 v;
-  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+  asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
   return v;
 }
 
@@ -117,59 +113,25 @@ __global__ void GALWORK_MIXED_BOUNDS mixed_kernel(Alloc *alloc, uint64_t n, uint
         n16 = size / 16;
       }
     }
-    // The warp fills and verifies its 32 allocations together: their 16-byte
-    // chunks are numbered across the warp in lane order, and step k covers
-    // chunks [32k, 32k + 32), one per lane, so every step is a coalesced
-    // 512-byte access that can span several allocations. Every byte of
-    // every allocation is written with its owner's (tid ^ round) and read
-    // back from L2 by the lane that wrote it. kFillSteps steps are stored
-    // before their loads are consumed, so that many loads are in flight at
-    // once rather than one allocation's at a time; mismatches are kept per
-    // owner in a mask and reduced once.
+    // The warp fills and verifies each lane's allocation in turn, 32 lanes x
+    // 16 bytes per step: every byte of every allocation is written with its
+    // owner's (tid ^ round) and read back from L2. Mismatches are collected
+    // per buffer in a mask and reduced once, so the loads of all 32 buffers
+    // can be in flight together.
     uint32_t mismatch = 0;
-    {
-      const uint32_t cnt = (uint32_t)n16;  // chunks of this lane's allocation (<= 256)
-      uint32_t incl = cnt;
-#pragma unroll
-      for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
+    for (uint32_t j = 0; j < 32; ++j) {
+      ulonglong2 *pj = (ulonglong2 *)__shfl_sync(0xffffffffu, (unsigned long long)p, j);
+      const uint64_t nj = __shfl_sync(0xffffffffu, n16, j);
+      const uint64_t vj = __shfl_sync(0xffffffffu, v, j);
+      if (pj == nullptr) continue;
+      const ulonglong2 fill = make_ulonglong2(vj, vj);
+      for (uint64_t i = lane; i < nj; i += 32) pj[i] = fill;
+      uint64_t diff = 0;
+      for (uint64_t i = lane; i < nj; i += 32) {
+        const ulonglong2 got = load_cg(pj + i);
+        diff |= (got.x ^ vj) | (got.y ^ vj);
       }
-      const uint32_t excl = incl - cnt;
-      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-      const uint32_t nonempty = __ballot_sync(0xffffffffu, cnt != 0);
-      const uint64_t tid0 = tid - lane;     // the warp's lanes hold consecutive tids
-      const uint32_t upto = 0xFFFFFFFFu >> (31 - lane);  // bits 0..lane
-      uint32_t ord_base = 0;  // allocations that start before the current step
-      for (uint32_t base = 0; base < total; base += 32 * kFillSteps) {
-        ulonglong2 *at[kFillSteps];
-        uint64_t val[kFillSteps];
-        uint32_t own[kFillSteps];
-#pragma unroll
-        for (uint32_t u = 0; u < kFillSteps; ++u) {
-          const uint32_t s0 = base + 32 * u;
-          // bit i: an allocation starts at chunk s0 + i
-          const uint32_t starts =
-              __reduce_or_sync(0xffffffffu, (cnt != 0 && excl >= s0 && excl - s0 < 32) ? 1u << (excl - s0) : 0u);
-          const uint32_t ord = ord_base + (uint32_t)__popc(starts & upto);  // 1-based, in lane order
-          ord_base += (uint32_t)__popc(starts);
-          const uint32_t owner = ord ? (__fns(nonempty, 0, (int)ord) & 31u) : 0u;
-          ulonglong2 *pj = (ulonglong2 *)__shfl_sync(0xffffffffu, (unsigned long long)p, (int)owner);
-          const uint32_t ej = __shfl_sync(0xffffffffu, excl, (int)owner);
-          const uint32_t g = s0 + lane;
-          own[u] = g < total ? owner : 32u;  // 32: no chunk for this lane in this step
-          at[u] = pj + (g - ej);
-          val[u] = (tid0 + owner) ^ r;
-          if (g < total) *at[u] = make_ulonglong2(val[u], val[u]);
-        }
-#pragma unroll
-        for (uint32_t u = 0; u < kFillSteps; ++u) {
-          if (own[u] < 32) {
-            const ulonglong2 got = load_cg(at[u]);
-            if ((got.x ^ val[u]) | (got.y ^ val[u])) mismatch |= 1u << own[u];
-          }
-        }
-      }
+      mismatch |= (uint32_t)(diff != 0) << j;
     }
     if ((__reduce_or_sync(0xffffffffu, mismatch) >> lane) & 1u) ++bad;
     if (p != nullptr) alloc->free(p);

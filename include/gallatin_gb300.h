@@ -249,6 +249,43 @@ int gal_run_mixed_host_noalloc(gal_allocator *h, uint64_t n_threads, uint32_t ro
                                uint32_t seg_every, uint64_t seg_lo, uint64_t seg_hi, const uint8_t *h_classes,
                                uint32_t block_dim, uint64_t *h_stats, void *stream);
 
+/* --- benchmark driver of the per-thread workloads (no reference
+ *     counterpart: the reference's tests time one launch with a host clock
+ *     around cudaDeviceSynchronize, timer.cuh:44-78) ---
+ * `warmup` untimed launches, then `steps` timed ones: before each, a write
+ * of flush_bytes (larger than L2, so no step starts with a warm L2), then
+ * the launch between two CUDA events on `stream`; step_ms[i] is its device
+ * time. With h_classes (a pinned host class trace, mixed workload only) the
+ * same steps then run end to end through gal_run_mixed_host (trace copied
+ * in, stats copied out, stream synchronised) with a host clock around each:
+ * e2e_step_ms[i]. stats / e2e_stats: the workload's stats words summed over
+ * the timed steps ([0] NULLs, [1] verify failures, [2]/[3] segment-tier
+ * successes / NULLs). */
+#define GAL_BENCH_PAIRS 0 /* gal_run_pairs(n_threads, size, block_dim) */
+#define GAL_BENCH_MIXED 1 /* gal_run_mixed(n_threads, rounds, seed, seg_*, d_classes, block_dim) */
+typedef struct gal_bench_args_t {
+  uint32_t workload;
+  uint32_t block_dim;
+  uint64_t n_threads;
+  uint64_t size;      /* pairs: bytes per malloc */
+  uint32_t rounds;    /* mixed */
+  uint32_t seg_every; /* mixed: segment-tier request every seg_every-th CTA (0 = none) */
+  uint64_t seed;
+  uint64_t seg_lo, seg_hi;
+  const uint8_t *d_classes; /* mixed: device class trace, or NULL (generated on the device) */
+  const uint8_t *h_classes; /* mixed: pinned host class trace for the end-to-end leg, or NULL */
+  uint32_t warmup, steps;
+  uint64_t flush_bytes;
+  void *stream;
+} gal_bench_args_t;
+typedef struct gal_bench_result_t {
+  float *step_ms;     /* caller buffer of `steps` floats */
+  float *e2e_step_ms; /* caller buffer of `steps` floats, or NULL without the end-to-end leg */
+  uint64_t stats[8];
+  uint64_t e2e_stats[8];
+} gal_bench_result_t;
+int gal_bench(gal_allocator *h, const gal_bench_args_t *args, gal_bench_result_t *out);
+
 /* --- device-first allocation with a host-arena fallback ---
  * The reference pairs a device allocator with one over pinned host memory
  * and offers global_malloc_fused / global_free_fused: malloc from the device
@@ -444,6 +481,12 @@ typedef struct gal_veb_op {
 #define GAL_VEB_OP_GATHER 11            /* gather_multiple(arg)          veb.cuh:1160 */
 #define GAL_VEB_OP_RETURN 12            /* return_multiple(arg, arg2)    veb.cuh:1198 */
 #define GAL_VEB_OP_REPORT_FILL 13       /* set leaf bits                 veb.cuh:1052 */
+/* The allocator's own searches (no reference counterpart; the reference's
+ * allocator uses find_random_valid_index and malloc_first): valid on trees
+ * whose upper layers are the OR of their children, i.e. trees changed only
+ * by INSERT_FORCE and REMOVE. */
+#define GAL_VEB_OP_FIND_AT_OR_AFTER 14  /* smallest set id >= arg, or ~0 */
+#define GAL_VEB_OP_CLAIM_FIRST 15       /* remove and return the smallest set id, or ~0 */
 
 /* Full tree over [0, universe) (reference veb_tree::generate_on_device). */
 int gal_veb_create(uint64_t universe, uint64_t seed, gal_veb **out);

@@ -242,7 +242,7 @@ __device__ inline void seg_avail_add_one(const gal_state_t *st, uint64_t seg) {
 // when a segment of t has several blocks, so that concurrent requests do not
 // each format one; every step is atomic on its own.
 __device__ inline uint64_t attach_segment(const gal_state_t *st, uint32_t t) {
-  const uint64_t seg = veb::malloc_first(&st->segment_tree);
+  const uint64_t seg = veb::claim_first(&st->segment_tree);  // smallest free id (reference malloc_first)
   if (seg == veb::kFail) return veb::kFail;
   unsigned short prev = atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)GAL_FREE_SEGMENT,
                                   (unsigned short)t);
@@ -282,14 +282,19 @@ __device__ inline uint32_t take_block(const gal_state_t *st, uint64_t seg, uint3
   if (before == 1) sub_tree_sync(st, t, seg);
   uint64_t *words = st->seg_block_bits + seg * st->seg_block_words;
   const int bis = block_index_shift(st);
+  // the segment's words are read in aligned pairs (seg_block_words is even)
   for (int pass = 0; pass < 64; ++pass) {
-    for (uint32_t w = 0; w < st->seg_block_words; ++w) {
-      uint64_t v = ptx::ld_relaxed(words + w);
-      while (v) {
-        const uint64_t bit = v & (~v + 1);
-        const uint64_t old = ptx::atom_and_acquire(words + w, ~bit);
-        if (old & bit) return (uint32_t)((seg << bis) + w * 64 + (uint64_t)(__ffsll((long long)bit) - 1));
-        v = old & ~bit;
+    for (uint32_t w = 0; w < st->seg_block_words; w += 2) {
+      uint64_t pair[2];
+      ptx::ld_relaxed_v2(words + w, pair[0], pair[1]);
+      for (uint32_t h = 0; h < 2; ++h) {
+        uint64_t v = pair[h];
+        while (v) {
+          const uint64_t bit = v & (~v + 1);
+          const uint64_t old = ptx::atom_and_acquire(words + w + h, ~bit);
+          if (old & bit) return (uint32_t)((seg << bis) + (w + h) * 64 + (uint64_t)(__ffsll((long long)bit) - 1));
+          v = old & ~bit;
+        }
       }
     }
   }
@@ -315,12 +320,17 @@ __device__ inline void return_block_to_segment(const gal_state_t *st, uint64_t b
   clear_nomem(st);
 }
 
-// A block belongs in class k's adoptable tree exactly while it is DETACHED
-// and serves class k, and in class k's roomy tree while in addition its live
-// count is at most GAL_ROOMY_MARK (same apply-then-confirm discipline as
-// sub_tree_sync: the last change to the facts is always applied).
+// A block belongs in class k's adoptable tree exactly while it is DETACHED,
+// serves class k and has room (live below a full block: a block of the
+// largest tree holds whole runs, so that is room for one more run), and in
+// class k's roomy tree while in addition its live count is at most
+// GAL_ROOMY_MARK (same apply-then-confirm discipline as sub_tree_sync: the
+// last change to the facts is always applied). Full detached blocks stay off
+// the adoptable tree, so an adopter's bounded scan does not spend itself on
+// them; the free that gives such a block room lists it again.
 __device__ __forceinline__ bool adopt_listed(uint64_t m, uint32_t k, bool roomy) {
-  return meta_state(m) == GAL_STATE_DETACHED && meta_class(m) == k && (!roomy || meta_live(m) <= GAL_ROOMY_MARK);
+  return meta_state(m) == GAL_STATE_DETACHED && meta_class(m) == k && meta_live(m) < GAL_BLOCK_SLICES &&
+         (!roomy || meta_live(m) <= GAL_ROOMY_MARK);
 }
 
 __device__ inline void adopt_sync(const gal_state_t *st, uint32_t k, uint64_t b, bool roomy) {
@@ -369,9 +379,13 @@ __device__ inline void after_release(const gal_state_t *st, uint64_t b, uint32_t
   const uint32_t live = meta_live(old);
   if (live == n) {
     try_retire_block(st, b);
-  } else if (meta_state(old) == GAL_STATE_DETACHED && live > GAL_ROOMY_MARK && live - n <= GAL_ROOMY_MARK) {
-    adopt_sync(st, meta_class(old), b, true);
+    return;
   }
+  if (meta_state(old) != GAL_STATE_DETACHED) return;
+  // a full detached block got room (also the undo of a reservation that
+  // found the block already detached): list it as adoptable again
+  if (live >= GAL_BLOCK_SLICES && live - n < GAL_BLOCK_SLICES) adopt_sync(st, meta_class(old), b, false);
+  if (live > GAL_ROOMY_MARK && live - n <= GAL_ROOMY_MARK) adopt_sync(st, meta_class(old), b, true);
 }
 
 __device__ __forceinline__ void release_live(const gal_state_t *st, uint64_t b, uint32_t n, bool ordered = false) {
@@ -421,13 +435,13 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
   const gal_veb_t *at = roomy ? &st->roomy_trees[k] : &st->adopt_trees[k];
   if (!veb_maybe_nonempty(at)) return GAL_EMPTY_BLOCK;
   const uint64_t start = murmur64a_u64(tid, at->seed) % at->universe;
-  uint64_t cand = veb::query(at, start) ? start : veb::successor_thorough(at, start);
+  uint64_t cand = veb::find_at_or_after(at, start);
   bool wrapped = false;
   for (int n = 0; n < kAdoptCandidates; ++n) {
     if (cand == veb::kFail) {
       if (wrapped) break;
       wrapped = true;
-      cand = veb::find_first_valid_index(at);
+      cand = veb::find_at_or_after(at, 0);
       if (cand == veb::kFail) break;
     }
     uint64_t m = ptx::ld_relaxed(st->block_meta + cand);
@@ -445,7 +459,7 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
       m = r;
     }
     if (!adopt_listed(m, k, roomy)) adopt_sync(st, k, cand, roomy);
-    cand = veb::successor_thorough(at, cand);
+    cand = veb::find_at_or_after(at, cand + 1);
   }
   return GAL_EMPTY_BLOCK;
 }
@@ -469,7 +483,7 @@ __device__ inline GAL_COLD uint32_t request_block(const gal_state_t *st, uint32_
   const gal_veb_t *sub = &st->sub_trees[t];
   int a = 0;
   for (; a < kRequestBlockAttempts; ++a) {
-    uint64_t seg = veb::find_random_valid_index(sub, mix_tid(tid, a));
+    uint64_t seg = veb::find_hashed(sub, mix_tid(tid, a));
     if (seg == veb::kFail) {
       // a segment of one block serves exactly one request: no lock needed
       const bool solo = (st->blocks_per_segment >> t) == 1;
@@ -480,7 +494,7 @@ __device__ inline GAL_COLD uint32_t request_block(const gal_state_t *st, uint32_
       seg = attach_segment(st, t);
       if (!solo) unlock(st, (int)t);
       if (seg == veb::kFail) {
-        if (veb::find_first_valid_index(sub) != veb::kFail) continue;
+        if (veb::find_at_or_after(sub, 0) != veb::kFail) continue;
         break;  // no formatted segment with a free block, no free segment
       }
     }
@@ -542,8 +556,16 @@ __device__ inline GAL_COLD int replace_slot(const gal_state_t *st, uint64_t *slo
   *out = GAL_EMPTY_BLOCK;
   if (atomicCAS((unsigned long long *)slot, seen, seen | GAL_SLOT_REPLACING) != seen) return REPLACE_BUSY;
   bool adopted = false;
-  const uint32_t nb = request_block(st, t, t + r, 1u << r, tid, adopt_mode, &adopted);
+  uint32_t nb = request_block(st, t, t + r, 1u << r, tid, adopt_mode, &adopted);
   const uint32_t kbit = 1u << (t + r);
+  if (nb == GAL_EMPTY_BLOCK && adopt_mode == ADOPT_ANY) {
+    // before the class is declared out of memory: a reservation that found
+    // its block already detached is undone one round trip later, and until
+    // then that block can look full to an adopter. Look once more.
+    __nanosleep(2000);
+    nb = adopt_block(st, t + r, 1u << r, tid, false);
+    adopted = nb != GAL_EMPTY_BLOCK;
+  }
   if (nb == GAL_EMPTY_BLOCK) {
     ptx::st_release(slot, seen);
     if (adopt_mode == ADOPT_ANY && !(ptx::ld_relaxed(st->nomem) & kbit)) atomicOr(st->nomem, kbit);
@@ -649,7 +671,18 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           }
           if (take == 0) {
             if (strikes) {
-              nomem = true;  // the arena had no block for the class: do not ask again
+              // the arena had no block for the class: do not ask again. But a
+              // block can look full only because another group's reservation
+              // on it is pending and about to be undone (two groups after the
+              // last slices can each see the other's): look again, and strike
+              // only a block with no room; one with room is tried again (in
+              // strike mode the slot index does not move)
+              const uint64_t again = ptx::ld_relaxed(st->block_meta + b);
+              if (meta_tag(again) == tag && meta_live(again) + c <= GAL_BLOCK_SLICES) {
+                busy = true;
+              } else {
+                nomem = true;
+              }
             } else if (!replacing) {
               count(st, GAL_CTR_REPLACE_FULL);
               uint32_t nb;

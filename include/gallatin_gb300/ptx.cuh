@@ -17,6 +17,10 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+// Two adjacent words (16-byte aligned) in one 128-bit load.
+__device__ __forceinline__ void ld_relaxed_v2(const uint64_t *p, uint64_t &lo, uint64_t &hi) {
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(lo), "=l"(hi) : "l"(p) : "memory");
+}
 __device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
   uint64_t v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");

@@ -244,6 +244,78 @@ __device__ __forceinline__ uint64_t malloc_random(const gal_veb_t *t, uint64_t t
   return lock_offset(t, 0);
 }
 
+// ---- searches of the allocator's own trees ------------------------------
+//
+// The allocator maintains its trees with insert_force_update and remove
+// only, so every upper-layer bit is the OR of its child word (up to the
+// moment of a concurrent change). On such a tree the smallest set id >= x is
+// one well-defined answer, and these searches reach it in fewer dependent
+// loads than query + successor_thorough: the query and the first leaf scan
+// share one load, which reads the aligned pair of leaf words holding x
+// (layers are allocated with an even number of words), so a successor in the
+// next word needs no float up; upper layers are visited only past the pair.
+// The op-for-op reference semantics above stay the parity surface.
+
+// Smallest set id >= x, or kFail. A word found empty on the way down (a
+// concurrent remove) resumes the search after it; the loop is bounded.
+__device__ inline uint64_t find_at_or_after(const gal_veb_t *t, uint64_t x) {
+  if (x >= t->universe) return kFail;
+  const int leaf = t->num_layers - 1;
+  const uint64_t w = x >> 6;
+  uint64_t p0, p1;
+  ptx::ld_relaxed_v2(word_ptr(t, leaf, w & ~1ull), p0, p1);
+  const uint64_t cur = ((w & 1) ? p1 : p0) & (~0ull << (x & 63));
+  if (cur) return (w << 6) + (uint64_t)(__ffsll((long long)cur) - 1);
+  if (!(w & 1) && p1) return ((w + 1) << 6) + (uint64_t)(__ffsll((long long)p1) - 1);
+  // search after word `idx` of `layer`
+  int layer = leaf;
+  uint64_t idx = w | 1;
+  for (int iter = 0; iter < kThoroughLimit; ++iter) {
+    // float up to the first layer whose word holds a set bit after idx's
+    while (true) {
+      if (layer == 0) return kFail;
+      const uint64_t pw = idx >> 6;
+      const int pb = (int)(idx & 63);
+      const uint64_t v = pb == 63 ? 0ull : (ptx::ld_relaxed(word_ptr(t, layer - 1, pw)) & (~0ull << (pb + 1)));
+      layer -= 1;
+      if (v) {
+        idx = (pw << 6) + (uint64_t)(__ffsll((long long)v) - 1);
+        layer += 1;  // idx is now a word of the child layer
+        break;
+      }
+      idx = pw;
+    }
+    // float down along first set bits
+    while (true) {
+      const uint64_t v = ptx::ld_relaxed(word_ptr(t, layer, idx));
+      if (v == 0) break;  // emptied meanwhile: search after it
+      const uint64_t b = (uint64_t)(__ffsll((long long)v) - 1);
+      if (layer == leaf) return (idx << 6) + b;
+      idx = (idx << 6) + b;
+      layer += 1;
+    }
+  }
+  return kFail;
+}
+
+// Claim the smallest set id (remove it), or kFail when none is set.
+__device__ inline uint64_t claim_first(const gal_veb_t *t) {
+  for (int iter = 0; iter < kThoroughLimit; ++iter) {
+    const uint64_t x = find_at_or_after(t, 0);
+    if (x == kFail) return kFail;
+    if (remove(t, x)) return x;
+  }
+  return kFail;
+}
+
+// A set id from a hashed start (MurmurHash64A of tid under the tree's seed,
+// as find_random_valid_index starts), wrapping to the smallest set id.
+__device__ inline uint64_t find_hashed(const gal_veb_t *t, uint64_t tid) {
+  const uint64_t start = murmur64a_u64(tid, t->seed) % t->universe;
+  const uint64_t x = find_at_or_after(t, start);
+  return (x != kFail || start == 0) ? x : find_at_or_after(t, 0);
+}
+
 // ---- contiguous runs (segment tier) -------------------------------------
 
 __device__ __forceinline__ uint64_t run_mask(int lo, int len) {

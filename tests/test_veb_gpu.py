@@ -80,3 +80,59 @@ def test_live_differential_against_reference_build(cuda, universe):
     assert np.array_equal(got, want)
     for a, b in zip(got_layers, want_layers):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("universe", [1, 64, 65, 127, 4097, 70000, 300000])
+def test_allocator_searches_match_a_brute_force_model(cuda, universe):
+    """The allocator's own searches (find_at_or_after, claim_first) on a tree
+    changed only by insert_force_update and remove (as the allocator's are):
+    every answer equals the smallest set id >= the argument in a set model,
+    including leaf words read in pairs past odd word counts, and the layers
+    end equal to the oracle's for the same insert/remove sequence."""
+    rng = np.random.default_rng(universe + 5)
+    n = 3000
+    ops = np.zeros(n, dtype=oracle.VEB_OP_DTYPE)
+    ops["code"] = rng.choice([1, 2, 14, 15], size=n, p=[0.35, 0.35, 0.25, 0.05])
+    ops["arg"] = rng.integers(0, universe, size=n, dtype=np.uint64)
+    # a third of the searches start at the last bit of a word
+    edge = rng.random(n) < 0.33
+    ops["arg"][edge] = np.minimum(
+        (rng.integers(0, max(universe // 64, 1), size=int(edge.sum())) * 64 + 63).astype(np.uint64),
+        np.uint64(universe - 1))
+    # thin the full tree first so the searches cross empty words and layers
+    pre = np.zeros(universe, dtype=oracle.VEB_OP_DTYPE)
+    pre["code"] = 2
+    pre["arg"] = np.arange(universe, dtype=np.uint64)
+    keep = rng.random(universe) < 0.05
+    pre = pre[~keep]
+    seq = np.concatenate([pre, ops])
+    res, layers = run_device(cuda, universe, 3, seq)
+    present = np.zeros(universe, dtype=bool)
+    present[keep] = True
+    fail = np.uint64((1 << 64) - 1)
+    for i, op in enumerate(seq):
+        code, arg = int(op["code"]), int(op["arg"])
+        got = res[i]
+        if code == 1:
+            assert bool(got) == (not present[arg])
+            present[arg] = True
+        elif code == 2:
+            assert bool(got) == bool(present[arg])
+            present[arg] = False
+        else:
+            start = 0 if code == 15 else arg
+            idx = np.flatnonzero(present[start:])
+            want = np.uint64(start + idx[0]) if idx.size else fail
+            assert got == want, f"op {i} ({code}, {arg}): got {int(got)}, want {int(want)}"
+            if code == 15 and idx.size:
+                present[start + idx[0]] = False
+    # the final layers equal the oracle's after the same inserts and removes
+    # (each successful claim is a remove of the id it returned)
+    claims = seq["code"] == 15
+    model_ops = seq.copy()
+    model_ops["code"][claims] = 2
+    model_ops["arg"][claims] = res[claims]
+    model_ops = model_ops[(model_ops["code"] != 14) & ~(claims & (res == fail))]
+    _, want_layers, _ = oracle.veb_run(universe, 3, oracle.MODE_GB300, model_ops)
+    for got, want in zip(layers, want_layers):
+        assert np.array_equal(got, want)
