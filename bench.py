@@ -268,9 +268,13 @@ def make_allocator(impl: str, w: dict, host: bool = False):
         return oracle.RefGallatin(size, seed, w["segment"], w["min_size"], w["max_size"], host_arena=host)
     import gallatin_gb300 as gal
 
-    make = gal.Gallatin.generate_on_device_host if host else gal.Gallatin.generate_on_device
-    return make(size, seed, print_info=False, running_calloc=bool(w.get("calloc")), segment_size=w["segment"],
-                min_size=w["min_size"], max_size=w["max_size"])
+    if host:
+        return gal.Gallatin.generate_on_device_host(size, seed, print_info=False, running_calloc=bool(w.get("calloc")),
+                                                    segment_size=w["segment"], min_size=w["min_size"],
+                                                    max_size=w["max_size"])
+    return gal.Gallatin.generate_on_device(size, seed, print_info=False, running_calloc=bool(w.get("calloc")),
+                                           segment_size=w["segment"], min_size=w["min_size"], max_size=w["max_size"],
+                                           drop_freed=bool(w.get("drop_freed")))
 
 
 def close_allocator(impl: str, a) -> None:
@@ -441,6 +445,8 @@ def run(args) -> dict | None:
         w["buckets"] = max(args.keys // 4, 1)
     if args.vectors and "vectors" in w:
         w["vectors"] = args.vectors
+    if args.drop_freed:
+        w["drop_freed"] = True
     if args.batch_hi and "batches" in w:
         w["batch_hi"] = args.batch_hi
     impl = args.impl
@@ -786,6 +792,8 @@ def run(args) -> dict | None:
             if not args.no_e2e:
                 native["h_classes"] = h_trace.data_ptr()
         config["driver"] = "native (gal_bench: CUDA events on the launching stream)"
+    if impl == "gb300" and w.get("drop_freed"):
+        config["freed_lines"] = "GAL_FLAG_DROP_FREED: free drops freed 128 B-4 KiB slices' L2 lines without write-back"
 
     if native is None:
         for _ in range(args.warmup):
@@ -1040,6 +1048,8 @@ def main() -> int:
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="mixed")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--drop-freed", action="store_true",
+                    help="create our allocator with GAL_FLAG_DROP_FREED: free drops freed slices' L2 lines")
     ap.add_argument("--threads", type=int, default=0, help="override the thread count (small profiling cases)")
     ap.add_argument("--rounds", type=int, default=0, help="override the rounds of the mixed workload")
     ap.add_argument("--arena-gib", type=float, default=0.0, help="override the arena size")

@@ -57,6 +57,7 @@ GAL_SEG_GATE = -(1 << 28)
 NOALLOC_TRACE_MAX_BYTES = 2 << 20
 FLAG_HOST_ARENA = 1  # arena in pinned host memory mapped into the GPU
 FLAG_CALLOC = 2  # malloc returns zeroed bytes (zero on free)
+FLAG_DROP_FREED = 4  # free drops freed 128 B..4 KiB slices' L2 lines without write-back (off by default)
 
 OPS = {
     "insert": 0,
@@ -372,10 +373,13 @@ class Gallatin:
         min_size: int = 16,
         max_size: int = 4096,
         min_slots: int = 0,
+        drop_freed: bool = False,
     ) -> "Gallatin":
-        """running_calloc: every malloc returns zeroed bytes (zero on free)."""
-        return cls._generate(max_bytes, seed, print_info, FLAG_CALLOC if running_calloc else 0, segment_size,
-                             min_size, max_size, min_slots)
+        """running_calloc: every malloc returns zeroed bytes (zero on free).
+        drop_freed: free drops the L2 lines of freed 128 B..4 KiB slices
+        without writing them back (GAL_FLAG_DROP_FREED)."""
+        flags = (FLAG_CALLOC if running_calloc else 0) | (FLAG_DROP_FREED if drop_freed else 0)
+        return cls._generate(max_bytes, seed, print_info, flags, segment_size, min_size, max_size, min_slots)
 
     @classmethod
     def generate_on_device_host(

@@ -110,7 +110,7 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
                              uint64_t max_size, uint32_t min_slots, uint32_t flags, gal_allocator **out) {
   if (out == nullptr) return fail_invalid("out is NULL");
   *out = nullptr;
-  if (flags & ~(GAL_FLAG_HOST_ARENA | GAL_FLAG_CALLOC)) return fail_invalid("unknown flags");
+  if (flags & ~(GAL_FLAG_HOST_ARENA | GAL_FLAG_CALLOC | GAL_FLAG_DROP_FREED)) return fail_invalid("unknown flags");
   if (!is_pow2(segment_bytes) || !is_pow2(min_size) || !is_pow2(max_size))
     return fail_invalid("segment, min and max sizes must be powers of two");
   if (max_size < min_size) return fail_invalid("max_size < min_size");

@@ -174,6 +174,44 @@ __device__ __forceinline__ void backoff(int attempt) {
   __nanosleep(ns);
 }
 
+// ---- tree searches ------------------------------------------------------
+//
+// The allocator's searches of its own trees. By default they are the
+// reference's operations (successor_thorough, find_random_valid_index,
+// malloc_first), which read one word per load. With -DGAL_PAIR_SEARCH they
+// are veb::find_at_or_after and its relatives, which read the leaf in
+// aligned 128-bit word pairs and merge the query with the first scan. Both
+// give the same answers on a quiescent tree (tests/test_veb_gpu.py checks
+// the pair searches against a brute-force set model), but under contention
+// the pair searches made the exact-capacity and mixed-tier tests see more
+// NULLs (2-4 of 16 runs short, against none in 108 runs with the default),
+// for a reason not yet found, so they stay off.
+__device__ __forceinline__ uint64_t tree_at_or_after(const gal_veb_t *t, uint64_t x) {
+#ifdef GAL_PAIR_SEARCH
+  return veb::find_at_or_after(t, x);
+#else
+  if (x >= t->universe) return veb::kFail;
+  if (veb::query(t, x)) return x;
+  return veb::successor_thorough(t, x);
+#endif
+}
+
+__device__ __forceinline__ uint64_t tree_hashed(const gal_veb_t *t, uint64_t tid) {
+#ifdef GAL_PAIR_SEARCH
+  return veb::find_hashed(t, tid);
+#else
+  return veb::find_random_valid_index(t, tid);
+#endif
+}
+
+__device__ __forceinline__ uint64_t tree_claim_first(const gal_veb_t *t) {
+#ifdef GAL_PAIR_SEARCH
+  return veb::claim_first(t);
+#else
+  return veb::malloc_first(t);
+#endif
+}
+
 // ---- locks (bounded) -----------------------------------------------------
 
 __device__ __forceinline__ bool try_lock(const gal_state_t *st, int bit) {
@@ -242,7 +280,7 @@ __device__ inline void seg_avail_add_one(const gal_state_t *st, uint64_t seg) {
 // when a segment of t has several blocks, so that concurrent requests do not
 // each format one; every step is atomic on its own.
 __device__ inline uint64_t attach_segment(const gal_state_t *st, uint32_t t) {
-  const uint64_t seg = veb::claim_first(&st->segment_tree);  // smallest free id (reference malloc_first)
+  const uint64_t seg = tree_claim_first(&st->segment_tree);  // smallest free id (reference malloc_first)
   if (seg == veb::kFail) return veb::kFail;
   unsigned short prev = atomicCAS((unsigned short *)(st->chunk_ids + seg), (unsigned short)GAL_FREE_SEGMENT,
                                   (unsigned short)t);
@@ -435,13 +473,13 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
   const gal_veb_t *at = roomy ? &st->roomy_trees[k] : &st->adopt_trees[k];
   if (!veb_maybe_nonempty(at)) return GAL_EMPTY_BLOCK;
   const uint64_t start = murmur64a_u64(tid, at->seed) % at->universe;
-  uint64_t cand = veb::find_at_or_after(at, start);
+  uint64_t cand = tree_at_or_after(at, start);
   bool wrapped = false;
   for (int n = 0; n < kAdoptCandidates; ++n) {
     if (cand == veb::kFail) {
       if (wrapped) break;
       wrapped = true;
-      cand = veb::find_at_or_after(at, 0);
+      cand = tree_at_or_after(at, 0);
       if (cand == veb::kFail) break;
     }
     uint64_t m = ptx::ld_relaxed(st->block_meta + cand);
@@ -459,7 +497,7 @@ __device__ inline uint32_t adopt_block(const gal_state_t *st, uint32_t k, uint32
       m = r;
     }
     if (!adopt_listed(m, k, roomy)) adopt_sync(st, k, cand, roomy);
-    cand = veb::find_at_or_after(at, cand + 1);
+    cand = tree_at_or_after(at, cand + 1);
   }
   return GAL_EMPTY_BLOCK;
 }
@@ -483,7 +521,7 @@ __device__ inline GAL_COLD uint32_t request_block(const gal_state_t *st, uint32_
   const gal_veb_t *sub = &st->sub_trees[t];
   int a = 0;
   for (; a < kRequestBlockAttempts; ++a) {
-    uint64_t seg = veb::find_hashed(sub, mix_tid(tid, a));
+    uint64_t seg = tree_hashed(sub, mix_tid(tid, a));
     if (seg == veb::kFail) {
       // a segment of one block serves exactly one request: no lock needed
       const bool solo = (st->blocks_per_segment >> t) == 1;
@@ -494,7 +532,7 @@ __device__ inline GAL_COLD uint32_t request_block(const gal_state_t *st, uint32_
       seg = attach_segment(st, t);
       if (!solo) unlock(st, (int)t);
       if (seg == veb::kFail) {
-        if (veb::find_at_or_after(sub, 0) != veb::kFail) continue;
+        if (tree_at_or_after(sub, 0) != veb::kFail) continue;
         break;  // no formatted segment with a free block, no free segment
       }
     }
@@ -612,6 +650,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   bool done = false;
   uint32_t hops = 0;     // slots passed over while another leader replaced their block
   uint32_t strikes = 0;  // slots found full or empty once the arena had no block for the class
+  bool last_pass = false;  // the strikes were reset once before giving up
   for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
     const uint32_t grp = __ballot_sync(peers, !done);
     if (grp == 0) break;
@@ -644,7 +683,8 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           nomem = replace_slot(st, slot, sv, t, r, ADOPT_ANY, &b) == REPLACE_NOMEM;
         } else {
           count(st, GAL_CTR_SLOT_BUSY);
-          nomem = (ptx::ld_relaxed(st->nomem) >> k) & 1u;
+          // the last pass passes over busy slots until it can replace one
+          nomem = !last_pass && ((ptx::ld_relaxed(st->nomem) >> k) & 1u);
           busy = !nomem;
         }
       }
@@ -689,7 +729,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
               nomem = replace_slot(st, slot, (uint64_t)b, t, r, ADOPT_ANY, &nb) == REPLACE_NOMEM;
             } else {
               count(st, GAL_CTR_SLOT_BUSY);
-              nomem = (ptx::ld_relaxed(st->nomem) >> k) & 1u;
+              nomem = !last_pass && ((ptx::ld_relaxed(st->nomem) >> k) & 1u);
               busy = !nomem;
             }
           }
@@ -752,7 +792,19 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     b = __shfl_sync(grp, b, leader);
     cursor = __shfl_sync(grp, cursor, leader);
     if (b == kNoMemBlock) {
-      if (++strikes >= nslots) done = true;
+      if (++strikes >= nslots) {
+        // a strike looks only at pinned blocks. A block detached with room
+        // after the replacement that found nothing is pinned by nobody once
+        // every group strikes, so before giving up the group makes one more
+        // pass that starts as a normal one (its next full or empty slot is
+        // replaced, adopting such a block)
+        if (last_pass) {
+          done = true;
+        } else {
+          last_pass = true;
+          strikes = 0;
+        }
+      }
       continue;
     }
     if (b == kBusyBlock) {
@@ -974,6 +1026,54 @@ __device__ inline uint64_t allocation_span(const gal_state_t *st, uint64_t off) 
   return 0;
 }
 
+// ---- dropping freed bytes from L2 ----------------------------------------
+//
+// A freed allocation's bytes are dead, but the lines its owner wrote sit
+// dirty in L2 and are written back to HBM when evicted: for allocations that
+// live briefly (written, read, freed) that write-back is most of their HBM
+// traffic. free drops those lines instead (discard.global.L2), for single
+// slices of 128 B to 4 KiB: their lines are whole, aligned and owned by this
+// allocation alone (smaller slices share lines with their neighbours; larger
+// spans cost more discards than the write-back they save when, as for pages,
+// most of the span is never written). The discards come before the free's
+// fence, so the next owner, who acquires the slice after the free's release,
+// writes after them.
+constexpr int kDiscardMaxShift = 12;  // largest slice whose lines are dropped: 4 KiB
+
+// Bytes at arena offset `off` whose lines free may drop, or 0.
+__device__ __forceinline__ uint64_t discard_span(const gal_state_t *st, uint64_t off) {
+  if (off >= st->arena_bytes) return 0;
+  const uint64_t seg = off >> st->segment_shift;
+  const uint16_t id = st->chunk_ids[seg];
+  if (id >= (uint16_t)st->num_trees) return 0;
+  const int slice_shift = st->min_shift + (int)id;
+  if (slice_shift < 7 || slice_shift > kDiscardMaxShift) return 0;
+  if (id == (uint16_t)st->num_trees - 1) {
+    // a block of the largest tree serves runs of one length: drop only single slices
+    const int block_shift = st->block_shift_min + (int)id;
+    const uint64_t b = (seg << block_index_shift(st)) + ((off & (st->segment_bytes - 1)) >> block_shift);
+    if (meta_run(st->block_meta[b]) != 0) return 0;
+  }
+  return 1ull << slice_shift;
+}
+
+// Drop the lines of [p, p + bytes) for every lane of `active` with bytes != 0
+// (bytes a multiple of 128, p 128-byte aligned): the lanes issue one discard
+// per line, one lane's range at a time, 4 KiB per full-warp step.
+__device__ inline void discard_ranges(uint32_t active, char *p, uint64_t bytes) {
+  const uint32_t lane = ptx::laneid();
+  const uint32_t rank = (uint32_t)__popc(active & ((1u << lane) - 1u));
+  const uint32_t group = (uint32_t)__popc(active);
+  uint32_t pending = __ballot_sync(active, bytes != 0);
+  while (pending) {
+    const int src = __ffs((int)pending) - 1;
+    pending &= pending - 1;
+    char *q = (char *)__shfl_sync(active, (unsigned long long)p, src);
+    const uint64_t lines = __shfl_sync(active, (unsigned long long)bytes, src) >> 7;
+    for (uint64_t i = rank; i < lines; i += group) ptx::discard_l2(q + (i << 7));
+  }
+}
+
 // ---- public entry points -------------------------------------------------
 
 // `width` limits warp aggregation to tiles of 8, 16 or 32 lanes (the
@@ -991,6 +1091,9 @@ __device__ inline void free(const gal_state_t *st, void *ptr, uint32_t width = 3
   if (st->flags & GAL_FLAG_CALLOC)
     zero_ranges(__activemask(), (char *)ptr,
                 ptr == nullptr ? 0 : allocation_span(st, (uint64_t)((char *)ptr - st->memory)));
+  else if ((st->flags & (GAL_FLAG_HOST_ARENA | GAL_FLAG_DROP_FREED)) == GAL_FLAG_DROP_FREED)
+    discard_ranges(__activemask(), (char *)ptr,
+                   ptr == nullptr ? 0 : discard_span(st, (uint64_t)((char *)ptr - st->memory)));
   if (ptr == nullptr) return;
   const uint64_t off = (uint64_t)((char *)ptr - st->memory);
   if (off >= st->arena_bytes) {

@@ -63,6 +63,11 @@ __device__ __forceinline__ uint64_t atom_add_relaxed(uint64_t *p, uint64_t v) {
   return r;
 }
 __device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+// Drop the 128-byte line at p (128-byte aligned) from L2 without writing it
+// back: its bytes become indeterminate until written again.
+__device__ __forceinline__ void discard_l2(const void *p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
+}
 __device__ __forceinline__ uint64_t atom_and_acquire(uint64_t *p, uint64_t v) {
   uint64_t r;
   asm volatile("atom.acquire.gpu.global.and.b64 %0, [%1], %2;" : "=l"(r) : "l"(p), "l"(v) : "memory");

@@ -79,6 +79,10 @@
 #define GAL_FLAG_CALLOC 2u     /* arena zeroed at creation and every free zeroes its bytes before they
                                   can be handed out again, so malloc returns zeroed memory (reference
                                   running_calloc, gallatin.cuh:1306-1369) */
+#define GAL_FLAG_DROP_FREED 4u /* a free of one slice of 128 B to 4 KiB on an HBM arena (without
+                                  GAL_FLAG_CALLOC) drops the slice's lines from L2 without writing them
+                                  back: the bytes are dead, so HBM never sees them. Off by default: it
+                                  saves HBM writes but costs L2 requests (see gal::discard_ranges). */
 
 /* default bound on the segment-tier lock wait: 2^20 tries with a backoff of
  * up to ~1 us each, about a second */

@@ -255,3 +255,23 @@ def test_mixed_full_configuration_restores_the_initial_state(cuda):
         rep = a.check_restored()
         assert rep["restored"], rep
         check_restored(a)
+
+
+@pytest.mark.parametrize("drop_freed", [False, True], ids=["lines-kept", "lines-dropped"])
+def test_freed_lines_dropped_or_kept_leave_every_allocation_intact(cuda, drop_freed):
+    """With drop_freed, free drops the L2 lines of freed 128 B..4 KiB slices
+    (discard, no write-back); by default it leaves them. Either way every
+    byte each owner writes reads back (the next owner writes after the
+    discard), nothing is NULL, and the state restores."""
+    with gal.Gallatin.generate_on_device(2 << 30, 13, print_info=False, drop_freed=drop_freed) as a:
+        assert bool(a.flags & gal.FLAG_DROP_FREED) == drop_freed
+        stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
+        for rep in range(3):
+            a.run_mixed(1 << 18, 6, 100 + rep, stats.data_ptr(), seg_every=64, seg_lo=16 << 20, seg_hi=64 << 20)
+        a.run_pairs(1 << 20, 256, stats.data_ptr(), block_dim=1024)
+        cuda.cuda.synchronize()
+        st = stats.cpu().numpy()
+        assert st[0] == 0 and st[1] == 0, st
+        a.flush_pinned()
+        cuda.cuda.synchronize()
+        check_restored(a)

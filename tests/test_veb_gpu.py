@@ -107,8 +107,7 @@ def test_allocator_searches_match_a_brute_force_model(cuda, universe):
     pre = pre[~keep]
     seq = np.concatenate([pre, ops])
     res, layers = run_device(cuda, universe, 3, seq)
-    present = np.zeros(universe, dtype=bool)
-    present[keep] = True
+    present = np.ones(universe, dtype=bool)  # the tree starts full
     fail = np.uint64((1 << 64) - 1)
     for i, op in enumerate(seq):
         code, arg = int(op["code"]), int(op["arg"])
