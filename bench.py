@@ -56,7 +56,12 @@ WORKLOADS = {
     "pairs": dict(arena=2 * GIB, segment=16 * MIB, min_size=16, max_size=4096, threads=1_048_576, size=16, block=1024),
     # the batching configuration: 64 batches of 1k-512k requests, lognormal
     # sizes, 60/40 malloc/free over the live set, plus a drain batch
-    "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32, binned=True),
+    # form: how the stream is served, each captured once in a CUDA graph:
+    # "launches" (one launch per batch), "persistent" (one cooperative kernel
+    # over all batches) or "binned" (the same, each batch counting-sorted by
+    # size class first); --batch-form overrides it
+    "batches": dict(arena=8 * GIB, segment=16 * MIB, min_size=16, max_size=4096, batches=64, width=32,
+                    form="launches"),
     # the data-structure configuration: a chained hash table of 64M keys
     # (insert all, erase half, reinsert them) with 120 B nodes from a 128 B
     # minimum allocator, and 1M doubling vectors
@@ -371,6 +376,19 @@ def cpu_baseline(name: str, w: dict) -> dict:
     }
 
 
+BATCH_FORM_TEXT = {
+    "launches": "one launch per batch",
+    "persistent": "one persistent cooperative kernel over all batches, warps taking 32 requests at a time",
+    "binned": "one persistent cooperative kernel over all batches, each batch counting-sorted by size class on the "
+              "device",
+}
+
+
+def batch_form(form: str) -> dict:
+    """capture_batches / run_batches arguments of a batch form."""
+    return {"persistent": form != "launches", "binned": form == "binned"}
+
+
 def batch_prefix_rates(torch, a, reqs, offsets, slots, w, stats, flush, steps) -> dict:
     """This allocator on the sample the reference arm of the batching workload
     is timed on (the first batches plus a drain): the configured persistent
@@ -385,10 +403,10 @@ def batch_prefix_rates(torch, a, reqs, offsets, slots, w, stats, flush, steps) -
     bargs = (d_reqs.data_ptr(), d_offs.data_ptr(), poffs, d_table.data_ptr(), stats.data_ptr())
     out = {"sample": f"first {REF_BATCH_PREFIX} of {len(offsets) - 2} batches, then a drain batch", "requests": n}
     stream = torch.cuda.current_stream()
-    for name, persistent in (("persistent+graph", True), ("per-thread launches", False)):
+    for name, graphed in ((w["form"] + "+graph", True), ("per-thread launches", False)):
         graph = None
-        if persistent:
-            graph = a.capture_batches(*bargs, width=w["width"], persistent=True, binned=w["binned"])
+        if graphed:
+            graph = a.capture_batches(*bargs, width=w["width"], **batch_form(w["form"]))
             fn = lambda: graph.launch(stream.cuda_stream)  # noqa: E731
         else:
             fn = lambda: a.run_batches(*bargs, width=w["width"], persistent=False, stream=stream.cuda_stream)  # noqa: E731
@@ -449,6 +467,8 @@ def run(args) -> dict | None:
         w["drop_freed"] = True
     if args.batch_hi and "batches" in w:
         w["batch_hi"] = args.batch_hi
+    if args.batch_form and "form" in w:
+        w["form"] = args.batch_form
     impl = args.impl
     if impl == "reference":
         import oracle
@@ -594,14 +614,16 @@ def run(args) -> dict | None:
             e2e_step = None
             launches_per_step = int(np.count_nonzero(np.diff(offsets)))  # one per non-empty batch
         else:
-            graph = a.capture_batches(*bargs, width=w["width"], persistent=True, binned=w["binned"])
+            graph = a.capture_batches(*bargs, width=w["width"], **batch_form(w["form"]))
+            if w["form"] == "launches":
+                launches_per_step = int(np.count_nonzero(np.diff(offsets)))  # one per non-empty batch
 
             def step():
                 graph.launch(s_ptr)
 
             def e2e_step():
-                return a.run_batches_host(reqs, offsets, slots, width=w["width"], persistent=True,
-                                          binned=w["binned"], stream=s_ptr, reqs_ptr=h_reqs.data_ptr())
+                return a.run_batches_host(reqs, offsets, slots, width=w["width"], **batch_form(w["form"]),
+                                          stream=s_ptr, reqs_ptr=h_reqs.data_ptr())
 
         h2d = units * 8 + len(offsets) * 8
         config = {
@@ -612,8 +634,7 @@ def run(args) -> dict | None:
             "max_size": w["max_size"], "requests": units, "mallocs": info["mallocs"], "frees": info["frees"],
             "max_live": info["max_live"], "max_request_bytes": info["max_request_bytes"], "seed": 42,
             "path": ("reference: one launch per batch" if impl == "reference"
-                     else f"persistent cooperative kernel in a CUDA graph, aggregation width {w['width']}"
-                          + (", each batch counting-sorted by size class on the device" if w["binned"] else "")),
+                     else BATCH_FORM_TEXT[w["form"]] + f", captured once in a CUDA graph, aggregation width {w['width']}"),
             "l2": "flushed (256 MiB write) before every timed step",
         }
         if sample:
@@ -925,9 +946,14 @@ def run(args) -> dict | None:
         "gpu_launches": args.steps * launches_per_step,
         "misses": int(st[0]),
         "verify_failures": int(st[1]),
-        "segment_tier": {"ok": int(st[2]), "null": int(st[3])},
         "step_ms": times,
     }
+    if args.workload in ("mixed", "mixed-slices", "calloc"):
+        # stats words 2 and 3 of the mixed kernel: segment-tier requests served / NULL
+        result["segment_tier"] = {"ok": int(st[2]), "null": int(st[3])}
+    elif args.workload == "table":
+        # stats word 3 of the table kernel: nodes freed (compaction and clear) over the timed steps
+        result["nodes_freed"] = int(st[3])
     if args.workload == "table":
         # untimed check of the whole lifecycle: every key where it should be
         chk = torch.zeros(8, dtype=torch.int64, device="cuda")
@@ -1056,6 +1082,8 @@ def main() -> int:
     ap.add_argument("--autotune", action="store_true", help="batches workload: add the segment x width sweep")
     ap.add_argument("--batches", type=int, default=0, help="override the batch count (small profiling cases)")
     ap.add_argument("--batch-hi", type=int, default=0, help="override the largest batch size")
+    ap.add_argument("--batch-form", choices=sorted(BATCH_FORM_TEXT), default=None,
+                    help="batches workload: how the stream is served (default: the workload's form)")
     ap.add_argument("--no-prefix", action="store_true",
                     help="batches: skip the timing on the reference's sample; serving: skip the plain-path run")
     ap.add_argument("--serve-steps", type=int, default=0, help="override the serving workload's step count")

@@ -2,9 +2,10 @@
 
 Stage 1 sweeps the segment size {4, 16, 64} MiB, the warp-aggregation width
 {8, 16, 32} and the kernel form (persistent cooperative kernel, with or
-without per-batch binning by size class), each captured as a CUDA graph and
-replayed. Stage 2 sweeps the kernel geometry (CTAs of 256 threads per SM) at
-the best stage-1 point. The plain per-thread path (one launch per batch, no
+without per-batch binning by size class, or one launch per batch), each
+captured as a CUDA graph and replayed. Stage 2 sweeps the kernel geometry
+(CTAs of 256 threads per SM) at the best stage-1 point when that point is a
+persistent form. The plain per-thread path (one launch per batch, no
 graph) is timed beside each segment size. A configuration qualifies only if
 none of its mallocs returned NULL; the best qualifying one is reported.
 
@@ -23,7 +24,7 @@ from . import Gallatin
 
 SEGMENTS = (4 << 20, 16 << 20, 64 << 20)
 WIDTHS = (8, 16, 32)
-FORMS = ("persistent", "binned")
+FORMS = ("persistent", "binned", "launches")
 GEOMETRIES = (1, 2, 3, 4)
 
 
@@ -58,7 +59,7 @@ def autotune_batches(reqs: np.ndarray, offsets: np.ndarray, table_slots: int, *,
 
     def graph_row(a, seg, form, width, geometry):
         try:
-            g = a.capture_batches(*args, width=width, persistent=True, binned=form == "binned",
+            g = a.capture_batches(*args, width=width, persistent=form != "launches", binned=form == "binned",
                                   ctas_per_sm=geometry)
         except RuntimeError as e:  # more CTAs per SM than fit
             return {"path": form + "+graph", "segment_bytes": seg, "width": width, "ctas_per_sm": geometry,
@@ -94,12 +95,13 @@ def autotune_batches(reqs: np.ndarray, offsets: np.ndarray, table_slots: int, *,
 
     best = max(qualified(rows) or [r for r in rows if "ms" in r], key=lambda r: r["ops_per_s"])
     seg, form, width = best["segment_bytes"], best["path"].split("+")[0], best["width"]
-    a = Gallatin.generate_on_device(arena, seed, print_info=False, segment_size=seg, max_size=_max_size(seg))
-    try:
-        for geometry in geometries:
-            rows.append(graph_row(a, seg, form, width, geometry))
-    finally:
-        a.free_on_device()
+    if form != "launches":  # one launch per batch has no persistent grid to size
+        a = Gallatin.generate_on_device(arena, seed, print_info=False, segment_size=seg, max_size=_max_size(seg))
+        try:
+            for geometry in geometries:
+                rows.append(graph_row(a, seg, form, width, geometry))
+        finally:
+            a.free_on_device()
     best = max(qualified(rows) or [r for r in rows if "ms" in r], key=lambda r: r["ops_per_s"])
     plain = max((r for r in rows if r["path"] == "per-thread launches"), key=lambda r: r["ops_per_s"])
     return {"ops": n_ops, "best": best, "best_per_thread": plain, "results": rows}

@@ -22,18 +22,26 @@ int grow(void **p, uint64_t *have, uint64_t need, const char *what) {
   return GAL_OK;
 }
 
-// Scratch of the binned path, sized for the largest batch. Grown before a
-// launch or a capture, never inside one.
-int ensure_bin_scratch(gal_allocator *h, const uint64_t *h_offsets, uint32_t n_batches) {
+// u32 counters of the persistent paths: the binned path's bin counts and
+// cursors (4 x kBins), then one work counter per batch.
+uint64_t counter_words(uint32_t n_batches) { return 4ull * galwork::kBins + n_batches; }
+
+// Scratch of the persistent paths: the counters, and for the binned path the
+// sorted batch (sized for the largest batch). Grown before a launch or a
+// capture, never inside one.
+int ensure_batch_scratch(gal_allocator *h, const uint64_t *h_offsets, uint32_t n_batches, bool binned) {
   uint64_t most = 0;
   for (uint32_t b = 0; b < n_batches; ++b) {
     const uint64_t n = h_offsets[b + 1] - h_offsets[b];
     if (n > most) most = n;
   }
-  if (most > 0xFFFFFFFFull) return galcapi::fail_invalid("a batch of the binned path holds at most 2^32-1 requests");
-  int rc = grow((void **)&h->d_bsorted, &h->d_bsorted_bytes, most * 8 + 8, "cudaMalloc sorted batch");
-  if (rc != GAL_OK) return rc;
-  return grow((void **)&h->d_bbins, &h->d_bbins_bytes, 4ull * galwork::kBins * 4, "cudaMalloc batch bins");
+  // a warp takes 32 requests per atomic on a u32 counter: keep it far from wrapping
+  if (most > 0x7FFFFFFFull) return galcapi::fail_invalid("a batch of the persistent paths holds at most 2^31-1 requests");
+  if (binned) {
+    const int rc = grow((void **)&h->d_bsorted, &h->d_bsorted_bytes, most * 8 + 8, "cudaMalloc sorted batch");
+    if (rc != GAL_OK) return rc;
+  }
+  return grow((void **)&h->d_bbins, &h->d_bbins_bytes, counter_words(n_batches) * 4, "cudaMalloc batch counters");
 }
 
 // ctas_per_sm: kernel geometry, 0 = as many as fit (every CTA must be
@@ -65,16 +73,17 @@ int launch_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_o
     GAL_CUDA_TRY(cudaGetLastError(), "batch launch");
     return GAL_OK;
   }
+  int rc = ensure_batch_scratch(h, h_offsets, n_batches, mode == 2);
+  if (rc != GAL_OK) return rc;
+  GAL_CUDA_TRY(cudaMemsetAsync(h->d_bbins, 0, counter_words(n_batches) * 4, s), "batch counters reset");
+  uint32_t *bins = h->d_bbins;
+  uint32_t *work = h->d_bbins + 4 * galwork::kBins;
   if (mode == 1) {
-    void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats};
+    void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats, &work};
     return launch_cooperative(h, galwork::persistent_batches_kernel<gal_device_alloc>, ctas_per_sm, s, args);
   }
-  int rc = ensure_bin_scratch(h, h_offsets, n_batches);
-  if (rc != GAL_OK) return rc;
-  GAL_CUDA_TRY(cudaMemsetAsync(h->d_bbins, 0, 4ull * galwork::kBins * 4, s), "bins reset");
   uint64_t *sorted = h->d_bsorted;
-  uint32_t *bins = h->d_bbins;
-  void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats, &sorted, &bins};
+  void *args[] = {&a, &d_reqs, &d_offsets, &n_batches, &d_table, &width, &d_stats, &sorted, &bins, &work};
   return launch_cooperative(h, galwork::binned_batches_kernel<gal_device_alloc>, ctas_per_sm, s, args);
 }
 
@@ -106,8 +115,8 @@ extern "C" int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, con
     return galcapi::fail_invalid("NULL argument");
   if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
   if (mode > 2) return galcapi::fail_invalid(kModeError);
-  if (mode == 2) {
-    const int rc = ensure_bin_scratch(h, h_offsets, n_batches);  // no allocation inside the capture
+  if (mode != 0) {
+    const int rc = ensure_batch_scratch(h, h_offsets, n_batches, mode == 2);  // no allocation inside the capture
     if (rc != GAL_OK) return rc;
   }
   cudaStream_t s;

@@ -60,8 +60,12 @@ __device__ __forceinline__ ulonglong2 load_cg(const ulonglong2 *p) {
   return v;
 }
 
-template <class Alloc>
-__global__ void __launch_bounds__(1024, 1) pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size, unsigned long long *stats) {
+// MinBlocks: CTAs of 1024 threads per SM the kernel is compiled for (the
+// register budget); each allocator's instance takes the value it runs
+// fastest with.
+template <class Alloc, int MinBlocks = 1>
+__global__ void __launch_bounds__(1024, MinBlocks) pairs_kernel(Alloc *alloc, uint64_t n, uint64_t size,
+                                                                 unsigned long long *stats) {
   const uint64_t tid = (uint64_t)threadIdx.x + (uint64_t)blockIdx.x * blockDim.x;
   if (tid >= n) return;
   uint64_t *p = (uint64_t *)alloc->malloc(size);
@@ -191,20 +195,41 @@ __global__ void GALWORK_MIXED_BOUNDS batch_kernel(A *a, const uint64_t *reqs, ui
   if (misses) atomicAdd(stats + STAT_MISS, misses);
 }
 
+// Serve requests [0, n) of one batch: each warp takes the next 32 from the
+// batch's work counter (`work`, zero before the batch; one atomic per 32
+// requests) until none are left. Warps that meet slow requests (a block
+// replacement) take fewer, so the batch does not wait on a fixed share of a
+// slow warp: on the 64-batch stream the persistent kernel took 8.5 ms this
+// way and 10.5 ms with a fixed stride (larger grabs, 64 to 256 requests per
+// atomic, were slower still: 10.6 to 24.8 ms). `sorted`: the requests were
+// written in this launch (read past L1). Call with whole, converged warps.
+template <class A>
+__device__ __forceinline__ void serve_batch(A *a, const uint64_t *reqs, uint64_t n, uint32_t *work, uint64_t *table,
+                                            uint32_t width, bool sorted, unsigned long long &misses) {
+  const uint32_t lane = threadIdx.x & 31;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(work, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((uint64_t)base >= n) break;
+    const uint64_t i = (uint64_t)base + lane;
+    if (i < n) serve_request(a, sorted ? __ldcg(reqs + i) : reqs[i], table, width, misses);
+  }
+}
+
 // persistent path: every batch in one cooperative launch; the grid syncs
 // between batches (which also orders a batch's table writes before the next
-// batch's frees read them)
+// batch's frees read them). `work`: one counter per batch, zero at launch.
 template <class A>
-__global__ void GALWORK_MIXED_BOUNDS persistent_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets, uint32_t n_batches,
-                                          uint64_t *table, uint32_t width, unsigned long long *stats) {
+__global__ void GALWORK_MIXED_BOUNDS persistent_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets,
+                                                               uint32_t n_batches, uint64_t *table, uint32_t width,
+                                                               unsigned long long *stats, uint32_t *work) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t rank = grid.thread_rank();
   unsigned long long misses = 0;
   for (uint32_t b = 0; b < n_batches; ++b) {
-    const uint64_t hi = offsets[b + 1];
-    for (uint64_t i = offsets[b] + rank; i < hi; i += nthreads) serve_request(a, reqs[i], table, width, misses);
+    const uint64_t lo = offsets[b];
+    serve_batch(a, reqs + lo, offsets[b + 1] - lo, work + b, table, width, false, misses);
     grid.sync();
   }
   if (misses) atomicAdd(stats + STAT_MISS, misses);
@@ -229,12 +254,13 @@ __device__ __forceinline__ uint32_t request_bin(uint64_t req) {
 // `bins` is 4 x kBins u32, zero at launch: counts and cursors, double
 // buffered by batch parity. Requests are dealt to CTAs the same way in the
 // count and the scatter (i = first + rank + k * threads), so the per-CTA
-// counts kept in shared memory between the two phases stay valid.
+// counts kept in shared memory between the two phases stay valid. `work`:
+// one counter per batch for the serving phase, zero at launch.
 template <class A>
 __global__ void GALWORK_MIXED_BOUNDS binned_batches_kernel(A *a, const uint64_t *reqs, const uint64_t *offsets,
                                                            uint32_t n_batches, uint64_t *table, uint32_t width,
                                                            unsigned long long *stats, uint64_t *sorted,
-                                                           uint32_t *bins) {
+                                                           uint32_t *bins, uint32_t *work) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
   __shared__ uint32_t s_cnt[kBins];
@@ -279,7 +305,7 @@ __global__ void GALWORK_MIXED_BOUNDS binned_batches_kernel(A *a, const uint64_t 
     }
     grid.sync();
     // phase B: serve; recycle this parity's counters; count the next batch
-    for (uint64_t j = rank; j < hi - lo; j += nthreads) serve_request(a, __ldcg(sorted + j), table, width, misses);
+    serve_batch(a, sorted, hi - lo, work + b, table, width, true, misses);
     if (blockIdx.x == 0 && threadIdx.x < kBins) {
       hist[threadIdx.x] = 0;
       cursor[threadIdx.x] = 0;

@@ -771,9 +771,19 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
           } else {
             // past the first pass: the cursor must not look fresh after it wraps
             if (m & GAL_META_FRESH_BIT) ptx::red_and_relaxed(st->block_meta + b, ~GAL_META_FRESH_BIT);
-            // a reused block's free slices are scattered: start leaders at
-            // hashed positions so they do not all chase the same word
-            if (m & GAL_META_REUSED_BIT) cursor *= 0x9E3779B1u;
+            // Where the search starts. Allocations that live briefly come back
+            // roughly in the order they went out, so the slices after the
+            // cursor are the oldest and mostly free, and claiming them in
+            // order keeps a block's live bytes together. A block more than
+            // half live holds allocations that stay, freed in any order: the
+            // words after the cursor are the ones just handed out and still
+            // full (on the batching stream a claim walked 11 words on
+            // average), so such a block, and one pinned again after a detach
+            // (scattered by definition), starts each search at a hashed word.
+            // The mark sits at half a block because a block that switches
+            // between the two orders often (marks of 512 or 1024) loses
+            // both: hashed claims punch holes ahead of the cursor.
+            if ((m & GAL_META_REUSED_BIT) || meta_live(m) > GAL_ROOMY_MARK) cursor *= 0x9E3779B1u;
             cursor &= GAL_BLOCK_SLICES - 1;
           }
         } else {

@@ -40,8 +40,15 @@ int launch_batches(G *a, const uint64_t *d_reqs, const uint64_t *d_offsets, cons
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
   uint32_t width = 32;
-  return cudaLaunchKernelEx(&cfg, galwork::persistent_batches_kernel<G>, a, d_reqs, d_offsets, n_batches, d_table,
-                            width, stats) == cudaSuccess ? 0 : 2;
+  // one work counter per batch, zero at launch (stream-ordered scratch)
+  uint32_t *work = nullptr;
+  const size_t work_bytes = (size_t)n_batches * 4 + 4;
+  if (cudaMallocAsync((void **)&work, work_bytes, s) != cudaSuccess) return 2;
+  cudaMemsetAsync(work, 0, work_bytes, s);
+  const int rc = cudaLaunchKernelEx(&cfg, galwork::persistent_batches_kernel<G>, a, d_reqs, d_offsets, n_batches,
+                                    d_table, width, stats, work) == cudaSuccess ? 0 : 2;
+  cudaFreeAsync(work, s);
+  return rc;
 }
 
 }  // namespace

@@ -58,8 +58,14 @@ struct RefTree {
 };
 
 template <class G>
+#ifndef GALREF_PAIRS_MIN_BLOCKS
+#define GALREF_PAIRS_MIN_BLOCKS 1
+#endif
+
 int launch_pairs(G *dev, uint64_t n, uint64_t size, uint32_t block, unsigned long long *stats, cudaStream_t s) {
-  galwork::pairs_kernel<G><<<(unsigned)((n + block - 1) / block), block, 0, s>>>(dev, n, size, stats);
+  // GALREF_PAIRS_MIN_BLOCKS=2 compiles the reference's instance for two CTAs per SM
+  galwork::pairs_kernel<G, GALREF_PAIRS_MIN_BLOCKS><<<(unsigned)((n + block - 1) / block), block, 0, s>>>(dev, n, size,
+                                                                                                      stats);
   return launch_status();
 }
 
