@@ -57,8 +57,7 @@ extern "C" int gal_table_op(gal_table *tb, uint32_t op, const uint64_t *d_keys, 
   const bool per_bucket = op == GAL_TABLE_COMPACT || op == GAL_TABLE_CLEAR;
   const uint64_t items = per_bucket ? tb->t.nbuckets : n;
   if (items == 0) return GAL_OK;
-  galdswork::table_kernel<gal_device_alloc><<<galcapi::grid_for(items, kBlock), kBlock, 0, (cudaStream_t)stream>>>(
-      tb->t, d_keys, n, key_seed, op, d_stats);
+  galdswork::launch_table_op(tb->t, d_keys, n, key_seed, op, d_stats, items, kBlock, (cudaStream_t)stream);
   GAL_CUDA_TRY(cudaGetLastError(), "table launch");
   return GAL_OK;
 }

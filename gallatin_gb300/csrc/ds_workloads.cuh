@@ -28,10 +28,16 @@ __device__ __forceinline__ bool erased_half(uint64_t seed, uint64_t i) {
   return galwork::splitmix64(seed ^ (i * 0x9E3779B97F4A7C15ull)) & 1;
 }
 
-// One thread per key (ops on keys) or per bucket (compact, clear).
-template <class A>
+// One thread per key (ops on keys) or per bucket (compact, clear). The
+// operation is a template argument: each operation's kernel holds only its
+// own code, so the phases that never allocate (erase, query) do not carry the
+// registers and stack of the inlined malloc path (as one kernel over every
+// operation, this library's instance had a 160-byte stack frame, and its
+// erase phase, which stores nothing, wrote 3.7 times the reference's sectors
+// to L2).
+template <class A, uint32_t op>
 __global__ void GALWORK_MIXED_BOUNDS table_kernel(galds::chaining_table<A> t, const uint64_t *keys, uint64_t n,
-                                                  uint64_t seed, uint32_t op, unsigned long long *stats) {
+                                                  uint64_t seed, unsigned long long *stats) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long fail = 0, miss = 0, wrong = 0, freed = 0;
   if (op == OP_COMPACT || op == OP_CLEAR) {
@@ -61,6 +67,23 @@ __global__ void GALWORK_MIXED_BOUNDS table_kernel(galds::chaining_table<A> t, co
     if (miss) atomicAdd(stats + DS_MISS, miss);
     if (wrong) atomicAdd(stats + DS_WRONG, wrong);
     if (freed) atomicAdd(stats + DS_NODES_FREED, freed);
+  }
+}
+
+// Launch table operation `op` over `items` threads (keys, or buckets for
+// compact and clear).
+template <class A>
+inline void launch_table_op(const galds::chaining_table<A> &t, const uint64_t *keys, uint64_t n, uint64_t seed,
+                            uint32_t op, unsigned long long *stats, uint64_t items, unsigned block, cudaStream_t s) {
+  const unsigned grid = (unsigned)((items + block - 1) / block);
+  switch (op) {
+    case OP_INSERT: table_kernel<A, OP_INSERT><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    case OP_ERASE_HALF: table_kernel<A, OP_ERASE_HALF><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    case OP_REINSERT_HALF: table_kernel<A, OP_REINSERT_HALF><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    case OP_QUERY: table_kernel<A, OP_QUERY><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    case OP_COMPACT: table_kernel<A, OP_COMPACT><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    case OP_CLEAR: table_kernel<A, OP_CLEAR><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
+    default: table_kernel<A, OP_QUERY_AFTER_ERASE><<<grid, block, 0, s>>>(t, keys, n, seed, stats); break;
   }
 }
 

@@ -10,7 +10,11 @@
 //
 // Both are templates over the allocator type A (anything with device
 // malloc(bytes) / free(ptr)), so the same code runs over this library's
-// allocator and over others. Every loop is bounded.
+// allocator and over others. Every loop is bounded. The table's insert is
+// force-inlined: compiled as a call, it put a 152-byte stack frame and
+// register saves around every insert. The vector's growth stays
+// a call: inlined into push_back's loop it raised the loop's spills and the
+// vectors ran 29 % slower.
 //
 // Concurrency: inserts, erases and queries of distinct keys may run at once.
 // A query that races an insert of the same key can see the key before its
@@ -63,7 +67,7 @@ struct chaining_table {
 
   // Insert key -> val. Returns false only when a node was needed and the
   // allocator returned NULL (or the chain bound was hit).
-  __device__ bool insert(uint64_t key, uint64_t val) {
+  __device__ __forceinline__ bool insert(uint64_t key, uint64_t val) {
     block_type **link = heads + bucket(key);
     block_type *b = load_link(link);
     for (int hop = 0; hop < kMaxChain; ++hop) {

@@ -22,7 +22,7 @@ int launch_table(G *dev, void *heads, uint64_t nbuckets, uint64_t seed, uint32_t
   t.seed = seed;
   const uint64_t items = (op == 4 || op == 5) ? nbuckets : n;
   if (items == 0) return 0;
-  galdswork::table_kernel<G><<<(unsigned)((items + 255) / 256), 256, 0, s>>>(t, keys, n, key_seed, op, stats);
+  galdswork::launch_table_op(t, keys, n, key_seed, op, stats, items, 256, s);
   return launch_status();
 }
 

@@ -53,8 +53,8 @@ def test_batches_serve_stream_and_restore(cuda, persistent, binned, width):
         check_restored(a)
 
 
-@pytest.mark.parametrize("binned", [False, True])
-def test_graph_replay_repeats_the_stream(cuda, binned):
+@pytest.mark.parametrize("persistent,binned", [(False, False), (True, False), (True, True)])
+def test_graph_replay_repeats_the_stream(cuda, persistent, binned):
     reqs, offsets, slots, info = small_trace(7)
     with gal.Gallatin.generate_on_device(1 << 30, 4, print_info=False) as a:
         d_reqs = cuda.from_numpy(reqs.view(np.int64)).cuda()
@@ -62,7 +62,7 @@ def test_graph_replay_repeats_the_stream(cuda, binned):
         d_table = cuda.zeros(slots + 1, dtype=cuda.int64, device="cuda")
         stats = cuda.zeros(8, dtype=cuda.int64, device="cuda")
         with a.capture_batches(d_reqs.data_ptr(), d_offs.data_ptr(), offsets, d_table.data_ptr(),
-                               stats.data_ptr(), persistent=True, binned=binned) as g:
+                               stats.data_ptr(), persistent=persistent, binned=binned) as g:
             for _ in range(3):
                 g.launch()
             cuda.cuda.synchronize()
