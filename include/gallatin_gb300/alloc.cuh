@@ -196,10 +196,29 @@ __device__ __forceinline__ uint64_t tree_at_or_after(const gal_veb_t *t, uint64_
 #endif
 }
 
+__device__ __forceinline__ bool veb_maybe_nonempty(const gal_veb_t *v) {
+  for (uint64_t w = 0; w < v->layer_words[0]; ++w)
+    if (ptx::ld_relaxed(v->bits[0] + w)) return true;
+  return false;
+}
+
+// A tree whose top layer reads empty twice, 2 us apart. The reference's
+// searches make 15 attempts of several dependent loads each before they
+// report an empty tree (about 100 loads for a block replacement that finds
+// neither a sub-tree segment nor a free segment, the common case once the
+// arena is full); the second look covers an insert whose upper-layer bits are
+// still on their way up, which those attempts rode out by taking long.
+__device__ inline bool veb_seems_empty(const gal_veb_t *v) {
+  if (veb_maybe_nonempty(v)) return false;
+  __nanosleep(2000);
+  return !veb_maybe_nonempty(v);
+}
+
 __device__ __forceinline__ uint64_t tree_hashed(const gal_veb_t *t, uint64_t tid) {
 #ifdef GAL_PAIR_SEARCH
   return veb::find_hashed(t, tid);
 #else
+  if (veb_seems_empty(t)) return veb::kFail;
   return veb::find_random_valid_index(t, tid);
 #endif
 }
@@ -208,6 +227,7 @@ __device__ __forceinline__ uint64_t tree_claim_first(const gal_veb_t *t) {
 #ifdef GAL_PAIR_SEARCH
   return veb::claim_first(t);
 #else
+  if (veb_seems_empty(t)) return veb::kFail;
   return veb::malloc_first(t);
 #endif
 }
@@ -456,12 +476,6 @@ __device__ __forceinline__ void own_block(const gal_state_t *st, uint64_t b, uin
 
 __device__ __forceinline__ uint64_t mix_tid(uint64_t tid, int attempt) {
   return attempt == 0 ? tid : murmur64a_u64(tid, (uint64_t)attempt);
-}
-
-__device__ __forceinline__ bool veb_maybe_nonempty(const gal_veb_t *v) {
-  for (uint64_t w = 0; w < v->layer_words[0]; ++w)
-    if (ptx::ld_relaxed(v->bits[0] + w)) return true;
-  return false;
 }
 
 // Pin again a DETACHED block of class k (tree t, run length c slices): from
