@@ -281,6 +281,8 @@ def load(path: str | Path | None = None):
         "gal_veb_layer_words": (u64, [vp, i32]),
         "gal_veb_dump": (i32, [vp, i32, vp]),
         "gal_veb_run_ops": (i32, [vp, vp, u64, vp, vp]),
+        "gal_veb_load": (i32, [vp, vp, u64]),
+        "gal_veb_find_batch": (i32, [vp, vp, u64, vp, u32, vp]),
         "gal_last_error": (c_char_p, []),
     }
     for name, (res, args) in sigs.items():
@@ -801,6 +803,17 @@ class VebTree:
 
     def run_ops(self, d_ops: int, n: int, d_results: int, stream: int = 0) -> None:
         _check(load().gal_veb_run_ops(self._h, d_ops, n, d_results, stream))
+
+    def load(self, leaf_words: np.ndarray) -> None:
+        """Set the leaf layer (bit i of word w = id 64w + i) and rebuild every
+        upper layer as the OR of its children (gal_veb_load)."""
+        w = np.ascontiguousarray(leaf_words, dtype=np.uint64)
+        _check(load().gal_veb_load(self._h, w.ctypes.data, len(w)))
+
+    def find_batch(self, d_queries: int, n: int, d_out: int, staged: bool = True, stream: int = 0) -> None:
+        """d_out[i] = smallest set id >= d_queries[i], or ~0 (gal_veb_find_batch);
+        staged: upper layers from a per-CTA shared-memory copy."""
+        _check(load().gal_veb_find_batch(self._h, d_queries, n, d_out, 1 if staged else 0, stream))
 
 
 # -- global allocator (reference global_allocator.cuh:41-97) -----------------

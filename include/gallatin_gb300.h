@@ -505,6 +505,24 @@ int gal_veb_dump(gal_veb *v, int layer, uint64_t *host_dst);
  * and writes results[i]. d_ops/d_results are device buffers. */
 int gal_veb_run_ops(gal_veb *v, const gal_veb_op *d_ops, uint64_t n, uint64_t *d_results, void *stream);
 
+/* Replace the tree's contents: host_leaf holds the leaf layer's words (bit i
+ * of word w = id 64w + i; no bit at or past the universe), and every upper
+ * layer is rebuilt as the OR of its child words, the state insert_force_update
+ * keeps. No reference counterpart (the reference fills a tree by inserts).
+ * Synchronous. */
+int gal_veb_load(gal_veb *v, const uint64_t *host_leaf, uint64_t words);
+/* For each of n device queries x, d_out = the smallest set id >= x, or ~0
+ * (the result GAL_VEB_OP_FIND_AT_OR_AFTER gives), on a tree whose upper
+ * layers are the OR of their children and that nothing changes during the
+ * call. staged = 1: each CTA first copies the tree's upper layers (as many
+ * of the top layers as fit 192 KiB of shared memory) into shared memory and
+ * answers its queries from there, with the leaf words read in aligned
+ * 128-bit pairs; staged = 0: one thread per query reading every layer from
+ * global memory (veb::find_at_or_after). No reference counterpart: the
+ * reference answers one successor at a time (veb.cuh:836-916). */
+int gal_veb_find_batch(gal_veb *v, const uint64_t *d_queries, uint64_t n, uint64_t *d_out, uint32_t staged,
+                       void *stream);
+
 /* Last CUDA error text recorded by this library (static storage). */
 const char *gal_last_error(void);
 

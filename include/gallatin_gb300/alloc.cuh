@@ -656,7 +656,10 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   const uint32_t lane = ptx::laneid();
   const uint32_t lt = ptx::lanemask_lt();
   const uint32_t nslots = st->slot_count[k];
-  const uint32_t slot0 = ptx::smid() % nslots;
+  // (integer remainders by a run-time count are long sequences: skipped when
+  // the value is already in range, the common case)
+  const uint32_t sm = ptx::smid();
+  const uint32_t slot0 = sm < nslots ? sm : sm % nslots;
   uint64_t *const slots = st->slots + st->slot_offset[k];
   // tree, state and run fields of a block pinned for this class
   const uint32_t tag = t | (GAL_STATE_PINNED << (GAL_META_STATE_SHIFT - 32)) | (r << (GAL_META_RUN_SHIFT - 32));
@@ -675,8 +678,9 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     const uint32_t need = g_n * c;
     // after a miss each slot is visited once, in order from slot0 + 1, so a
     // strike on every slot means every slot was seen full or empty
-    uint64_t *const slot =
-        slots + (strikes ? (slot0 + strikes) % nslots : (slot0 + (uint32_t)(attempt >> 3) + hops) % nslots);
+    uint32_t slot_i = strikes ? slot0 + strikes : slot0 + (uint32_t)(attempt >> 3) + hops;
+    if (slot_i >= nslots) slot_i %= nslots;
+    uint64_t *const slot = slots + slot_i;
 
     uint32_t b = GAL_EMPTY_BLOCK;
     uint32_t cursor = 0;
@@ -859,11 +863,23 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     uint32_t w = cursor >> 6;
     uint32_t lo = ((cursor & 63) + c - 1) & ~(c - 1);
     uint64_t avail = lo >= 64 ? 0ull : (~0ull << lo);
+    // avail is still a whole range [lo, 64) (nothing learned about the word
+    // yet): its lowest runs are its first (take - acc) * c bits, taken at
+    // once instead of one run at a time (a warp's group of 32 single slices
+    // spent 32 loop turns here)
+    bool whole = true;
     for (int step = 0; step < kClaimSteps && acc < take; ++step) {
       uint64_t got = 0;
       uint32_t gw = w;
       if (lane == (uint32_t)leader) {
-        const uint64_t pick = lowest_bits(run_starts(avail, c), take - acc);
+        uint64_t pick;
+        if (whole) {
+          const uint32_t from = avail ? (uint32_t)(__ffsll((long long)avail) - 1) : 64u;
+          const uint32_t span = (take - acc) * c;
+          pick = run_starts(span >= 64 - from ? avail : (((1ull << span) - 1) << from), c);
+        } else {
+          pick = lowest_bits(run_starts(avail, c), take - acc);
+        }
         if (pick) {
           const uint64_t mask = expand_runs(pick, c);
           const uint64_t old = ptx::atom_and_acquire(bits + w, ~mask);
@@ -878,9 +894,11 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
         } else {
           avail = 0;
         }
+        whole = false;
         if (run_starts(avail, c) == 0) {
           w = (w + 1) & 63;
           avail = ~0ull;
+          whole = true;
         }
       }
       got = ptx::shfl64(grp, got, leader);
