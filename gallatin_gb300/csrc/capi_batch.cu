@@ -167,6 +167,32 @@ extern "C" int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, co
     return rc;
   cudaStream_t s = (cudaStream_t)stream;
   GAL_CUDA_TRY(cudaMemsetAsync(h->d_stats, 0, 64, s), "stats reset");
+  if (mode == 0 && valid_width(width)) {
+    // one launch per batch: batch b's requests are copied on a side stream
+    // while the batches before it run, and its launch waits for its copy
+    if (h->copy_stream == nullptr)
+      GAL_CUDA_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), "copy stream");
+    if (h->copy_event == nullptr)
+      GAL_CUDA_TRY(cudaEventCreateWithFlags(&h->copy_event, cudaEventDisableTiming), "copy event");
+    // the copies overwrite the scratch only after earlier work on `s` that may read it
+    GAL_CUDA_TRY(cudaEventRecord(h->copy_event, s), "copy event record");
+    GAL_CUDA_TRY(cudaStreamWaitEvent(h->copy_stream, h->copy_event, 0), "copy stream wait");
+    gal_device_alloc *a = reinterpret_cast<gal_device_alloc *>(h->d_state);
+    for (uint32_t b = 0; b < n_batches; ++b) {
+      const uint64_t lo = h_offsets[b], n = h_offsets[b + 1] - lo;
+      if (n == 0) continue;
+      GAL_CUDA_TRY(cudaMemcpyAsync(h->d_breqs + lo, h_reqs + lo, n * 8, cudaMemcpyHostToDevice, h->copy_stream),
+                   "batch requests H2D");
+      GAL_CUDA_TRY(cudaEventRecord(h->copy_event, h->copy_stream), "copy event record");
+      GAL_CUDA_TRY(cudaStreamWaitEvent(s, h->copy_event, 0), "batch waits for its copy");
+      galwork::batch_kernel<gal_device_alloc><<<galcapi::grid_for(n, kBatchBlock), kBatchBlock, 0, s>>>(
+          a, h->d_breqs + lo, n, h->d_btable, width, h->d_stats);
+    }
+    GAL_CUDA_TRY(cudaGetLastError(), "batch launch");
+    GAL_CUDA_TRY(cudaMemcpyAsync(h_stats, h->d_stats, 64, cudaMemcpyDeviceToHost, s), "stats D2H");
+    GAL_CUDA_TRY(cudaStreamSynchronize(s), "batch e2e sync");
+    return GAL_OK;
+  }
   GAL_CUDA_TRY(cudaMemcpyAsync(h->d_breqs, h_reqs, nreq * 8, cudaMemcpyHostToDevice, s), "requests H2D");
   GAL_CUDA_TRY(cudaMemcpyAsync(h->d_boffs, h_offsets, (n_batches + 1) * 8ull, cudaMemcpyHostToDevice, s),
                "offsets H2D");

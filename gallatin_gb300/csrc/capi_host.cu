@@ -138,6 +138,8 @@ extern "C" int gal_create_ex(uint64_t max_bytes, uint64_t seed, uint64_t segment
   h->d_stats = nullptr;
   h->d_breqs = h->d_boffs = h->d_btable = nullptr;
   h->d_breqs_bytes = h->d_boffs_bytes = h->d_btable_bytes = 0;
+  h->copy_stream = nullptr;
+  h->copy_event = nullptr;
   h->d_bsorted = nullptr;
   h->d_bbins = nullptr;
   h->d_bsorted_bytes = h->d_bbins_bytes = 0;
@@ -298,6 +300,8 @@ extern "C" int gal_destroy(gal_allocator *h) {
   if (h->d_serve) cudaFree(h->d_serve);
   if (h->d_ftable) cudaFree(h->d_ftable);
   if (h->d_fused) cudaFree(h->d_fused);
+  if (h->copy_event) cudaEventDestroy(h->copy_event);
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
   free_all(h->device_allocs);
   if (h->host_arena) cudaFreeHost(h->host_arena);
   delete h;

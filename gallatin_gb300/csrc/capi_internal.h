@@ -26,6 +26,10 @@ struct gal_allocator {
   uint64_t d_boffs_bytes;
   uint64_t *d_btable;
   uint64_t d_btable_bytes;
+  // the host-buffer batch path's copy stream and event (made on first use):
+  // batch b's requests are copied while earlier batches run
+  cudaStream_t copy_stream;
+  cudaEvent_t copy_event;
   // scratch of the binned batch path: one sorted batch, bin counters
   uint64_t *d_bsorted;
   uint64_t d_bsorted_bytes;
