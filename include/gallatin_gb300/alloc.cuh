@@ -251,6 +251,13 @@ __device__ __forceinline__ void unlock(const gal_state_t *st, int bit) {
 // stable, so the last change always wins. Under contention a segment can be
 // listed without a free block for a moment (searches then fail on it and
 // sync it again); it is never left unlisted while it has a free block.
+// The fences around each apply make "last" mean what it says: a fact change
+// is ordered before its author's membership update, and a membership update
+// that lands after another one (they are read-modify-writes of one word) is
+// ordered before its author's re-read, which therefore sees the other
+// author's fact change. Without them the re-read could return a fact older
+// than a retire whose remove it had just overwritten, and leave a retired
+// segment listed.
 __device__ __forceinline__ bool seg_listed_for(const gal_state_t *st, uint32_t t, uint64_t seg) {
   return ptx::ld_relaxed(st->chunk_ids + seg) == t && ptx::ld_relaxed(st->seg_avail + seg) > 0;
 }
@@ -259,11 +266,13 @@ __device__ inline void sub_tree_sync(const gal_state_t *st, uint32_t t, uint64_t
   const gal_veb_t *sub = &st->sub_trees[t];
   bool want = seg_listed_for(st, t, seg);
   for (int i = 0; i < 8; ++i) {
+    ptx::fence_acq_rel();
     if (want) {
       veb::insert_force_update(sub, seg);
     } else {
       veb::remove(sub, seg);
     }
+    ptx::fence_acq_rel();
     const bool now = seg_listed_for(st, t, seg);
     if (now == want) return;
     want = now;
