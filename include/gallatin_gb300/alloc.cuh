@@ -676,6 +676,7 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
   bool done = false;
   uint32_t hops = 0;     // slots passed over while another leader replaced their block
   uint32_t strikes = 0;  // slots found full or empty once the arena had no block for the class
+  uint32_t missed = 0;   // slot index (before the remainder) of the last visit outside strike mode
   bool last_pass = false;  // the strikes were reset once before giving up
   for (int attempt = 0; attempt < kSliceAttempts; ++attempt) {
     const uint32_t grp = __ballot_sync(peers, !done);
@@ -685,9 +686,18 @@ __device__ __forceinline__ void *malloc_slice(const gal_state_t *st, uint32_t t,
     const uint32_t g_n = __popc(grp);
     const uint32_t g_rank = __popc(grp & lt);
     const uint32_t need = g_n * c;
-    // after a miss each slot is visited once, in order from slot0 + 1, so a
-    // strike on every slot means every slot was seen full or empty
-    uint32_t slot_i = strikes ? slot0 + strikes : slot0 + (uint32_t)(attempt >> 3) + hops;
+    // after a miss each other slot is visited once, in order from the
+    // missed one, so a strike on every slot means every slot was seen full
+    // or empty. (The miss is not always at slot0: after busy hops, or eight
+    // attempts on one slot, a group has moved on, and counting from slot0
+    // left slot0 unvisited.)
+    uint32_t slot_i;
+    if (strikes) {
+      slot_i = missed + strikes;
+    } else {
+      slot_i = slot0 + (uint32_t)(attempt >> 3) + hops;
+      missed = slot_i;
+    }
     if (slot_i >= nslots) slot_i %= nslots;
     uint64_t *const slot = slots + slot_i;
 
