@@ -6,7 +6,8 @@
 * oracle/_ref/include/...         the reference's hot-path headers, copied
                                   unmodified from the reference checkout (an
                                   install step: the reference is header-only
-                                  CUDA, and the GPU machine has no checkout)
+                                  CUDA, and a machine that runs the GPU
+                                  tests need not have the checkout)
 * oracle/_ref/libgalref_<family>.so
                                   the harness (ref_core.cu, ref_batches.cu,
                                   ref_serving.cu, ref_ds.cu, ref_fused.cu)
@@ -14,8 +15,9 @@
                                   one library per family so they build in
                                   parallel
 
-Everything lands in git-ignored folders. The GPU machine rebuilds from the staged
-headers, since binaries built on this x86 host do not run there. The
+Everything lands in git-ignored folders. A machine of another architecture
+rebuilds from the staged headers, since binaries built elsewhere do not run
+there. The
 reference checkout is read from $GALLATIN_REFERENCE, else /root/reference.
 """
 from __future__ import annotations
