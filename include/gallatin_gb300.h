@@ -515,7 +515,7 @@ int gal_veb_load(gal_veb *v, const uint64_t *host_leaf, uint64_t words);
  * (the result GAL_VEB_OP_FIND_AT_OR_AFTER gives), on a tree whose upper
  * layers are the OR of their children and that nothing changes during the
  * call. staged = 1: each CTA first copies the tree's upper layers (as many
- * of the top layers as fit 192 KiB of shared memory) into shared memory and
+ * of the top layers as fit 48 KiB of shared memory) into shared memory and
  * answers its queries from there, with the leaf words read in aligned
  * 128-bit pairs; staged = 0: one thread per query reading every layer from
  * global memory (veb::find_at_or_after). No reference counterpart: the

@@ -63,6 +63,20 @@ def test_create_ex_rejects_unknown_flags_without_touching_the_gpu():
     assert b"flags" in lib.gal_last_error()
 
 
+def test_veb_batch_entry_points_reject_bad_arguments_without_touching_the_gpu():
+    import gallatin_gb300 as gal
+
+    lib = gal.load()
+    assert lib.gal_veb_load(None, None, 0) == 1
+    assert b"NULL" in lib.gal_last_error()
+    assert lib.gal_veb_find_batch(None, None, 1, None, 1, None) == 1
+    assert b"NULL" in lib.gal_last_error()
+    # the form is checked before the handle is read
+    handle = ctypes.create_string_buffer(8)
+    assert lib.gal_veb_find_batch(ctypes.addressof(handle), None, 0, None, 2, None) == 1
+    assert b"staged" in lib.gal_last_error()
+
+
 def test_owns_allocation_is_the_arena_range():
     import gallatin_gb300 as gal
 
