@@ -90,6 +90,22 @@ int launch_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_o
 bool valid_width(uint32_t w) { return w == 8 || w == 16 || w == 32; }
 constexpr const char *kModeError = "mode must be 0 (per batch), 1 (persistent) or 2 (persistent, binned)";
 
+// Batch b is requests [offsets[b], offsets[b + 1]): the offsets must not
+// decrease, or a launch would read past the request buffer. Checked on the
+// host before anything is allocated or launched.
+int check_offsets(const uint64_t *h_offsets, uint32_t n_batches) {
+  for (uint32_t b = 0; b < n_batches; ++b)
+    if (h_offsets[b + 1] < h_offsets[b]) return galcapi::fail_invalid("batch offsets must not decrease");
+  return GAL_OK;
+}
+
+// The checks every batch entry point makes before it touches the GPU.
+int check_batch_args(const uint64_t *h_offsets, uint32_t n_batches, uint32_t width, uint32_t mode) {
+  if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
+  if (mode > 2) return galcapi::fail_invalid(kModeError);
+  return check_offsets(h_offsets, n_batches);
+}
+
 }  // namespace
 
 extern "C" int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets,
@@ -98,8 +114,8 @@ extern "C" int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const u
   if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
       d_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
-  if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
-  if (mode > 2) return galcapi::fail_invalid(kModeError);
+  const int rc = check_batch_args(h_offsets, n_batches, width, mode);
+  if (rc != GAL_OK) return rc;
   return launch_batches(h, d_reqs, d_offsets, h_offsets, n_batches, d_table, width, mode, ctas_per_sm, d_stats,
                         (cudaStream_t)stream);
 }
@@ -113,8 +129,7 @@ extern "C" int gal_capture_batches(gal_allocator *h, const uint64_t *d_reqs, con
   if (h == nullptr || d_reqs == nullptr || d_offsets == nullptr || h_offsets == nullptr || d_table == nullptr ||
       d_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
-  if (!valid_width(width)) return galcapi::fail_invalid("width must be 8, 16 or 32");
-  if (mode > 2) return galcapi::fail_invalid(kModeError);
+  if (const int rc = check_batch_args(h_offsets, n_batches, width, mode)) return rc;
   if (mode != 0) {
     const int rc = ensure_batch_scratch(h, h_offsets, n_batches, mode == 2);  // no allocation inside the capture
     if (rc != GAL_OK) return rc;
@@ -159,15 +174,16 @@ extern "C" int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, co
                                     uint32_t ctas_per_sm, uint64_t *h_stats, void *stream) {
   if (h == nullptr || h_reqs == nullptr || h_offsets == nullptr || h_stats == nullptr)
     return galcapi::fail_invalid("NULL argument");
+  int rc = check_batch_args(h_offsets, n_batches, width, mode);
+  if (rc != GAL_OK) return rc;
   const uint64_t nreq = h_offsets[n_batches];
-  int rc;
   if ((rc = grow((void **)&h->d_breqs, &h->d_breqs_bytes, nreq * 8 + 8, "cudaMalloc batch requests")) ||
       (rc = grow((void **)&h->d_boffs, &h->d_boffs_bytes, (n_batches + 1) * 8ull, "cudaMalloc batch offsets")) ||
       (rc = grow((void **)&h->d_btable, &h->d_btable_bytes, table_slots * 8 + 8, "cudaMalloc batch table")))
     return rc;
   cudaStream_t s = (cudaStream_t)stream;
   GAL_CUDA_TRY(cudaMemsetAsync(h->d_stats, 0, 64, s), "stats reset");
-  if (mode == 0 && valid_width(width)) {
+  if (mode == 0) {
     // one launch per batch: batch b's requests are copied on a side stream
     // while the batches before it run, and its launch waits for its copy
     if (h->copy_stream == nullptr)

@@ -329,14 +329,16 @@ int gal_run_zeroed(gal_allocator *h, uint64_t n_threads, uint32_t rounds, uint64
  *     serves per-thread calls from user kernels) ---
  * A request is a u64: slot << 32 | size; size > 0 mallocs into
  * table[slot], size 0 frees table[slot]. Batch b is requests
- * [offsets[b], offsets[b+1]). width (8, 16, 32) limits warp aggregation to
- * tiles of that many lanes. mode 0: one launch per batch (the plain
- * per-thread call path); mode 1: one cooperative persistent launch that
- * serves every batch with a grid barrier between batches; mode 2: as mode 1,
- * but each batch is first counting-sorted on the device by power-of-two size
- * class (frees first), so a warp's lanes share a class; the sort uses
- * scratch the handle owns, sized for the largest batch (at most 2^32-1
- * requests). ctas_per_sm: CTAs of 256 threads per SM for modes 1 and 2
+ * [offsets[b], offsets[b+1]); offsets that decrease, a width or a mode out
+ * of range give GAL_ERR_INVALID before anything is allocated or launched.
+ * width (8, 16, 32) limits warp aggregation to tiles of that many lanes.
+ * mode 0: one launch per batch (the plain per-thread call path); mode 1: one
+ * cooperative persistent launch that serves every batch with a grid barrier
+ * between batches; mode 2: as mode 1, but each batch is first
+ * counting-sorted on the device by power-of-two size class (frees first), so
+ * a warp's lanes share a class; the sort uses scratch the handle owns, sized
+ * for the largest batch. A batch of modes 1 and 2 holds at most 2^31-1
+ * requests. ctas_per_sm: CTAs of 256 threads per SM for modes 1 and 2
  * (kernel geometry; 0 = as many as fit, more is refused). stats as for the
  * workloads ([0] = mallocs that returned NULL). */
 int gal_run_batches(gal_allocator *h, const uint64_t *d_reqs, const uint64_t *d_offsets, const uint64_t *h_offsets,

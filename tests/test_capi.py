@@ -77,6 +77,35 @@ def test_veb_batch_entry_points_reject_bad_arguments_without_touching_the_gpu():
     assert b"staged" in lib.gal_last_error()
 
 
+def test_batch_entry_points_check_offsets_width_and_mode_without_touching_the_gpu():
+    import numpy as np
+
+    import gallatin_gb300 as gal
+
+    lib = gal.load()
+    # a handle that is never read: these checks come before any use of it
+    fake = ctypes.create_string_buffer(64)
+    h = ctypes.addressof(fake)
+    reqs = np.zeros(5, dtype=np.uint64)
+    stats = np.zeros(8, dtype=np.uint64)
+    bad = np.array([0, 5, 3], dtype=np.uint64)  # batch 1 would be [5, 3)
+    good = np.array([0, 3, 5], dtype=np.uint64)
+
+    def host(offsets, width=32, mode=0):
+        return lib.gal_run_batches_host(h, reqs.ctypes.data, offsets.ctypes.data, 2, 16, width, mode, 0,
+                                        stats.ctypes.data, None)
+
+    assert host(bad) == 1 and b"decrease" in lib.gal_last_error()
+    assert host(good, width=12) == 1 and b"width" in lib.gal_last_error()
+    assert host(good, mode=3) == 1 and b"mode" in lib.gal_last_error()
+    d = reqs.ctypes.data  # device pointers are passed through, never read by the checks
+    assert lib.gal_run_batches(h, d, d, bad.ctypes.data, 2, d, 32, 1, 0, d, None) == 1
+    assert b"decrease" in lib.gal_last_error()
+    graph = ctypes.c_void_p(1)
+    assert lib.gal_capture_batches(h, d, d, bad.ctypes.data, 2, d, 32, 0, 0, d, ctypes.byref(graph)) == 1
+    assert b"decrease" in lib.gal_last_error() and not graph.value
+
+
 def test_owns_allocation_is_the_arena_range():
     import gallatin_gb300 as gal
 
