@@ -353,7 +353,9 @@ int gal_graph_launch(void *graph_exec, void *stream);
 int gal_graph_destroy(void *graph_exec);
 /* End to end from host buffers: copies the requests and offsets to scratch
  * the handle owns (grown on demand), runs, copies the 8 stats words back and
- * synchronises `stream`. table_slots: size of the live-set table. */
+ * synchronises `stream`. table_slots: size of the live-set table; every
+ * request's slot must be below it (not checked: that would be a host pass
+ * over every request inside the call). */
 int gal_run_batches_host(gal_allocator *h, const uint64_t *h_reqs, const uint64_t *h_offsets, uint32_t n_batches,
                          uint64_t table_slots, uint32_t width, uint32_t mode, uint32_t ctas_per_sm,
                          uint64_t *h_stats, void *stream);
